@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""World-step benchmark (one JSON line on rank 0).
+
+Workload: the plain drop-in world step at full size -- a 2048x2048 world
+with a 2048x2048 fluid grid, multigrid pressure on 8 levels down to 16x16
+with 4 V-cycles of 3+3 red-black Gauss-Seidel sweeps (30 sweeps on the
+coarsest level), monomer transport and the exact-mass ledger every step,
+on seeded synthetic inputs (value-noise velocity, 10% rock, Poisson(4)
+monomers in 8 fields).  A step is one full world step (fluid + pressure +
+transport + ledger) of one world.
+
+  value  world-steps/s, device time (CUDA events on the world's stream),
+         state resident in HBM (~0.7 GB, larger than L2: every step
+         streams it, so no L2 flush is needed between steps)
+  e2e    the same metric through the public API with host buffers: per
+         step, SimParams go host->device and the step's ledger comes back
+         device->host and is checked against the seeded counts
+  --impl reference   the CPU restatement of the reference's passes (the
+         reference itself is Rust + WGSL on wgpu and cannot run here),
+         all host threads, bounded sample of the same workload
+N > 1 GPUs run independent replicas (one world per rank, no collective).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ribossome-v2_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "world-steps/s at 2048^2"
+UNIT = "world-steps/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_config(n):
+    return {
+        "workload": f"plain world step {n}x{n} (fluid {n}x{n}), multigrid 8 levels to 16x16, 4 V-cycles of 3+3 "
+                    "red-black GS sweeps, 30 coarse sweeps, transport + exact ledger every step",
+        "grid": [n, n], "fluid": [n, n], "mg_min_size": 16, "mg_cycles": 4, "mg_pre": 3, "mg_post": 3,
+        "mg_coarse": 30, "fluid_substep": 1, "transport_every": 1, "dt": 1.0,
+        "inputs": "seeded synthetic: 4-octave value-noise velocity (max 0.5 cells/step), 10% rock, "
+                  "Poisson(4) monomers x 8 fields",
+        "l2": "inputs larger than L2: ~0.7 GB of resident world state streamed every step",
+    }
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summaries."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for name in sorted(os.listdir(pdir)):
+        if not name.endswith((".txt", ".md")):
+            continue
+        for line in open(os.path.join(pdir, name)):
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == "traffic_bytes_per_launch:" and parts[1] == kernel:
+                try:
+                    return float(parts[2])
+                except ValueError:
+                    pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(n, seconds_budget=15.0, max_steps=20):
+    """The oracle (CPU restatement) on the host cores: a bounded sample of the workload."""
+    import ribo_oracle
+    import ribo_world as rw
+    import synth
+
+    threads = os.cpu_count() or 1
+    ribo_oracle.set_threads(threads)
+    o = ribo_oracle.OracleWorld(n, seed=1000, mg_min_size=16, mg_pre=3, mg_post=3)
+    o.seed_inputs(synth.make_world_inputs(n, seed=1000))
+    bp = synth.bench_params(1000)
+    for k, _ in rw.SimParams._fields_:
+        setattr(o.params, k, getattr(bp, k))
+    o.settings.fluid_substep = 1
+    o.settings.mg_cycles = 4
+    o.encode_steps(1)  # warm-up
+    t = time.perf_counter()
+    o.encode_steps(1)
+    one = time.perf_counter() - t
+    steps = int(max(1, min(max_steps, seconds_budget / max(one, 1e-6))))
+    t = time.perf_counter()
+    done = 0
+    while done < steps:
+        k = min(64, steps - done)
+        o.encode_steps(k)
+        done += k
+    el = time.perf_counter() - t
+    return {"value": steps / el, "unit": UNIT, "cores": ribo_oracle.get_threads(), "kind": "port",
+            "sample": f"{steps} full world steps of the {n}x{n} workload after 2 untimed steps ({el:.1f} s)"}
+
+
+def run_reference(args):
+    ws, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    import ribo_oracle
+    import ribo_world as rw
+    import synth
+
+    n = args.size
+    threads = os.cpu_count() or 1
+    ribo_oracle.set_threads(threads)
+    o = ribo_oracle.OracleWorld(n, seed=1000, mg_min_size=16, mg_pre=3, mg_post=3)
+    o.seed_inputs(synth.make_world_inputs(n, seed=1000))
+    bp = synth.bench_params(1000)
+    for k, _ in rw.SimParams._fields_:
+        setattr(o.params, k, getattr(bp, k))
+    o.settings.fluid_substep = 1
+    o.settings.mg_cycles = 4
+    warm = min(args.warmup, 2)
+    for _ in range(warm):
+        o.encode_steps(1)
+    t = time.perf_counter()
+    o.encode_steps(1)
+    one = time.perf_counter() - t
+    steps = int(max(1, min(args.steps - 1, args.reference_seconds / max(one, 1e-6))))
+    t = time.perf_counter()
+    done = 0
+    while done < steps:
+        k = min(64, steps - done)
+        o.encode_steps(k)
+        done += k
+    el = time.perf_counter() - t + one
+    steps += 1
+    value = steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
+        "warmup": warm, "ms_per_step": 1000.0 * el / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic", "config": workload_config(n),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": ribo_oracle.get_threads(), "kind": "port",
+                         "sample": f"{steps} of the {args.steps} requested full world steps ({el:.1f} s); the "
+                                   "reference (Rust + WGSL via wgpu) cannot run without a graphics stack, so its "
+                                   "passes run as the C++ restatement"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    ws, rank, local = dist_setup()
+    import ribo_world as rw
+    import synth
+
+    n = args.size
+    seed = 1000 + rank
+    inputs = synth.make_world_inputs(n, seed=seed)
+    w = rw.World(n, seed=seed, mg_min_size=16, mg_pre=3, mg_post=3, device=local)
+    w.params = synth.bench_params(seed)
+    w.settings.fluid_substep = 1
+    w.settings.mg_cycles = 4
+    w.settings.ledger_each_step = 1
+    w.seed_inputs(inputs)
+    seeded = rw.Ledger.from_cells(inputs[rw.CHEM])
+
+    def run_steps(k, timing=False, acc=None):
+        done = 0
+        while done < k:
+            c = min(rw.MAX_STEPS_PER_FRAME, k - done)
+            w.encode_steps(c)
+            done += c
+            if timing:
+                for name, launches, ms, b in w.read_kernel_timing():
+                    e = acc.setdefault(name, [0, 0.0, 0.0])
+                    e[0] += launches
+                    e[1] += ms
+                    e[2] += b
+            ledgers = w.step_ledgers(c)
+            if any(l != seeded for l in ledgers):
+                raise RuntimeError("matter not conserved")
+
+    run_steps(max(args.warmup, 3))
+    w.sync()
+    barrier(ws)
+
+    # ---- device-timed region ----
+    clocks = Clocks(local)
+    clocks.start()
+    w.enable_kernel_timing(True)
+    kern = {}
+    launches0 = rw.kernel_launch_count()
+    w.mark(0)
+    run_steps(args.steps, timing=True, acc=kern)
+    w.mark(1)
+    ms = w.elapsed_ms(0, 1)
+    launches = rw.kernel_launch_count() - launches0
+    w.enable_kernel_timing(False)
+    clk = clocks.stop()
+    barrier(ws)
+    ms_max = max_over_ranks(ws, ms)
+    value = args.steps * ws / (ms_max / 1000.0)
+
+    # ---- end to end through the public API, host buffers ----
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    w.sync()
+    barrier(ws)
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        w.encode_steps(1)
+        led = w.step_ledgers(1)[0]
+        if led != seeded:
+            raise RuntimeError("matter not conserved (e2e)")
+    el = time.perf_counter() - t
+    el = max_over_ranks(ws, el)
+    e2e = {"value": e2e_steps * ws / el, "unit": UNIT, "h2d_bytes_per_step": 464, "d2h_bytes_per_step": 48,
+           "note": "per step: SimParams host->device (encode_steps), then the step's ledger device->host and "
+                   "checked against the seeded counts; wall clock"}
+
+    # ---- roofline of the dominant kernel ----
+    peak, peak_kind = read_peaks()
+    top = max(kern.items(), key=lambda kv: kv[1][1])
+    name, (nl, tms, tb) = top
+    avg_ms = tms / nl
+    bpl = tb / nl
+    achieved = bpl / (avg_ms * 1e-3) / 1e9
+    traffic = profile_traffic(name)
+    step_bytes = sum(v[2] for v in kern.values()) / args.steps
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs (copy)",
+                "bytes_per_launch": bpl, "avg_launch_ms": avg_ms,
+                "share_of_step": tms / max(sum(v[1] for v in kern.values()), 1e-9)}
+    step_rl = {"bytes_per_step": step_bytes, "achieved": step_bytes / (ms / args.steps * 1e-3) / 1e9,
+               "frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}
+    breakdown = sorted(((k, v[1] / args.steps, v[0] // args.steps) for k, v in kern.items()), key=lambda x: -x[1])
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
+        "config": dict(workload_config(n), parallelism=f"replicas x{ws}" if ws > 1 else "single world"),
+        "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "step_roofline": step_rl,
+        "kernels_ms_per_step": [[k, round(t, 4), c] for k, t, c in breakdown[:12]],
+        "clocks": clk,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(n)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--e2e-steps", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-seconds", type=float, default=60.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,306 @@
+// C ABI of the GB300 world-step library (libribo_world.so).
+//
+// The library replaces the GPU side of the reference's world step: the
+// `World` methods in src/world/mod.rs that own the device buffers and record
+// the fluid / multigrid / transport / ledger dispatches.  Every entry point
+// takes plain pointers and sizes; nothing here depends on CUDA or PyTorch
+// headers.  A `ribo_world` handle is thread-affine (like the reference's
+// `World`, which is not Sync): all calls on one handle come from one thread,
+// and all device work of a handle is ordered on one CUDA stream.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Status codes.  Setup errors in the reference are `Result<_, String>`
+// (src/gpu/mod.rs:15-41); the text of the last error is kept per thread and
+// returned by ribo_last_error().
+typedef enum ribo_status {
+  RIBO_OK = 0,
+  RIBO_INVALID_ARG = 1,
+  RIBO_OOM = 2,
+  RIBO_OVER_BUDGET = 3,
+  RIBO_TIMEOUT = 4,
+  RIBO_CUDA_ERROR = 5,
+} ribo_status;
+
+// Per-step parameters: the reference's `SimParams` (src/params.rs:86-487),
+// 116 four-byte fields in the same order and with the same names, 464 bytes.
+// One copy per simulated step, as in the reference's uniform buffer
+// (src/world/mod.rs:1431-1445).  Only the fields the world hot path reads are
+// interpreted here; the others travel unchanged.
+typedef struct ribo_sim_params {
+  uint32_t  epoch;
+  uint32_t  seed;
+  float     dt;
+  float     diffusion;
+  float     settle;
+  float     fluid_dt;
+  float     fluid_decay;
+  float     fluid_vorticity;
+  float     fluid_viscosity;
+  uint32_t  fumarole_count;
+  float     uv_strength;
+  float     uv_depth;
+  uint32_t  fluid_enabled;
+  float     fluid_obstacle_strength;
+  float     slope_steer_rate;
+  float     cohesion;
+  uint32_t  spawn_count;
+  uint32_t  max_agents;
+  float     death_probability;
+  float     spawn_energy;
+  float     food_power;
+  float     maintenance_cost;
+  float     pairing_rate;
+  float     mutation_rate;
+  float     uv_damage;
+  float     uptake_rate;
+  float     brownian;
+  float     phoretic_gain;
+  float     chain_stiffness;
+  float     thermal_kt;
+  float     motor_amplitude;
+  uint32_t  rft_enabled;
+  uint32_t  require_start;
+  float     joint_coupling;
+  uint32_t  hunger_regulation;
+  float     pairing_cost;
+  float     reactivation_rate;
+  float     swim_gain;
+  float     bioturbation;
+  float     bioturbation_cost;
+  float     monomer_uv_absorb;
+  float     sedimentation;
+  float     direct_photoactivation;
+  float     activation_decay;
+  float     monomer_pressure;
+  float     agent_fluid_push;
+  float     swim_wobble;
+  uint32_t  fluid_swim_only;
+  float     motion_cost;
+  float     bond_rate;
+  float     bond_energy_share;
+  float     bond_signal;
+  float     aggregation;
+  float     photo_yield;
+  float     heat_kill;
+  float     flow_coupling;
+  float     inertia;
+  float     death_energy_cap;
+  float     chemo_yield;
+  float     redox_decay;
+  float     thermal_activation;
+  float     denature_temp;
+  float     day_period;
+  float     sun_slope;
+  float     sun_now;
+  float     sun_angle;
+  float     day_fraction;
+  float     metabolic_q10;
+  float     metabolic_span;
+  float     metabolic_ref;
+  float     sun_heat;
+  float     sediment_transport;
+  float     sediment_threshold;
+  float     sediment_settle;
+  float     signal_mode;
+  float     clock_mute;
+  float     paint_x;
+  float     paint_y;
+  float     paint_radius;
+  float     paint_grains;
+  float     rest_angle_mult;
+  float     protease_power;
+  float     lysis_yield;
+  float     protease_direct;
+  float     joint_load;
+  float     swim_grip;
+  float     swim_memory;
+  float     mouth_leak;
+  float     leak_base;
+  float     skin_uptake;
+  float     death_metab;
+  float     salvage;
+  float     bond_matter_share;
+  float     brownian_rot;
+  uint32_t  transport_every;
+  float     signal_crosstalk;
+  float     flow_mass;
+  float     chemo_take;
+  float     vent_cycle_period;
+  float     vent_cycle_amp;
+  float     sediment_cohesion;
+  float     sediment_compaction;
+  float     rock_crumble;
+  float     lysis_matter;
+  uint32_t  scramble_conduction;
+  uint32_t  scramble_angles;
+  uint32_t  scramble_response;
+  float     scramble_amount;
+  float     pairing_energy_half;
+  float     pairing_min_energy;
+  float     uv_mutation;
+  float     heat_mutation;
+  float     birth_crowding;
+  float     photo_damage;
+  float     naked_decay;
+  float     store_loss;
+} ribo_sim_params;
+
+// World dimensions and multigrid constants.  The reference fixes a square
+// GRID_SIZE / FLUID_SIZE at shader-compile time (src/shaders.rs:134-156,
+// src/params.rs:1006-1034) and the multigrid constants as Rust consts
+// (src/world/mod.rs:196-202); here they are runtime values.  grid_w/grid_h
+// may differ (rectangular worlds); grid_w/fluid_w must equal grid_h/fluid_h
+// and both must be integers >= 1.  Zero multigrid fields take the reference
+// values MG_PRE=2, MG_POST=2, MG_COARSE=30, MG_MIN_SIZE=8.
+typedef struct ribo_world ribo_world;
+
+typedef struct ribo_world_cfg {
+  uint32_t grid_w, grid_h;        // environment grid (GRID_SIZE)
+  uint32_t fluid_w, fluid_h;      // fluid grid (FLUID_SIZE)
+  uint32_t world_units_per_cell;  // 30 in WorldConfig::DEFAULT / TEST
+  uint32_t mg_min_size;           // coarsest multigrid side (MG_MIN_SIZE)
+  uint32_t mg_pre, mg_post;       // red-black sweeps before / after the coarse correction
+  uint32_t mg_coarse;             // red-black sweeps on the coarsest level
+  uint32_t precision_mode;        // RIBO_PRECISION_*
+  uint32_t device;                // CUDA device ordinal the world lives on
+  uint32_t reserved[5];
+} ribo_world_cfg;
+
+enum {
+  RIBO_PRECISION_F32 = 0,    // the reference's arithmetic (bit-exact with the oracle)
+  RIBO_PRECISION_MIXED = 1,  // fp16-storage fine-level smoothing, fp32 defect correction, fp64 coarse solve
+};
+
+// Host-side world settings that are not GPU parameters: the hot-path subset
+// of the reference's `WorldSettings` (src/world/mod.rs:94-134).
+typedef struct ribo_world_settings {
+  uint32_t fluid_enabled;  // run the fluid block
+  uint32_t fluid_substep;  // fluid every N steps with dt*N (clamped to 1..4)
+  uint32_t multigrid;      // 1 = multigrid pressure, 0 = Jacobi
+  uint32_t mg_cycles;      // V-cycles per fluid step (>= 1)
+  uint32_t jacobi_iters;   // Jacobi iterations (rounded to even, 2..128)
+  uint32_t ledger_each_step;  // 1 = run ledger_reduce after every step (read with ribo_world_step_ledgers)
+  uint32_t reserved[2];
+} ribo_world_settings;
+
+// Device fields a caller can upload / read.  Sizes in bytes, for a world with
+// C = grid_w*grid_h env cells, F = fluid_w*fluid_h fluid cells and
+// L = (grid_w/2)*(grid_h/2) light cells.
+typedef enum ribo_field {
+  RIBO_FIELD_CHEM = 0,           // C*16: 4 u32 per cell (A,U,G,C), low 16 bits activated, high 16 spent
+  RIBO_FIELD_GAMMA = 1,          // C*4:  grains per cell (>= 3 rock)
+  RIBO_FIELD_LIGHT = 2,          // 2*L*4: UV light, two bands (frozen input)
+  RIBO_FIELD_SLOPE = 3,          // C*8:  terrain slope (derived from GAMMA on upload)
+  RIBO_FIELD_VELOCITY = 4,       // F*8:  velocity_a (final velocity of a step)
+  RIBO_FIELD_PRESSURE = 5,       // F*4:  pressure_a (warm start of the next solve)
+  RIBO_FIELD_TEMP = 6,           // F*4:  temperature (temp_in)
+  RIBO_FIELD_REDOX = 7,          // F*4:  vent reductant (redox_in)
+  RIBO_FIELD_HEAT = 8,           // F*8:  vent heat / chemistry source per fluid cell
+  RIBO_FIELD_VEL_SMOOTH = 9,     // F*8:  5-point smoothed final velocity
+  RIBO_FIELD_SOLID_MASK = 10,    // F*4:  1 = wall (derived from GAMMA)
+  RIBO_FIELD_DIVERGENCE = 11,    // F*4:  last divergence
+  RIBO_FIELD_FORCE_VECTORS = 12, // F*8:  fixed-point (x256) force accumulators (agent pushes)
+  RIBO_FIELD_REDOX_EATEN = 13,   // F*4:  fixed-point reductant consumed by agents
+  RIBO_FIELD_NET_FLUX = 14,      // (fluid_h+fluid_w)*4: row means of v_y then column means of v_x
+  RIBO_FIELD_SHADE = 15,         // 2*L*4: agent shade per light cell (fixed point, 100 = one)
+  RIBO_FIELD_COUNT = 16,
+} ribo_field;
+
+// Last error text of the calling thread ("" if none).
+const char* ribo_last_error(void);
+
+// The reference defaults of SimParams (src/params.rs:553-690) and
+// WorldSettings (src/world/mod.rs:117-134).
+void ribo_sim_params_default(ribo_sim_params* out);
+void ribo_world_settings_default(ribo_world_settings* out);
+
+// World::new (src/world/mod.rs:416): allocates every device buffer of the
+// world step, zeroed.  Fails with RIBO_INVALID_ARG on bad sizes and RIBO_OOM
+// when device memory runs out.
+ribo_status ribo_world_create(const ribo_world_cfg* cfg, ribo_world** out);
+void ribo_world_destroy(ribo_world* w);
+
+ribo_status ribo_world_set_settings(ribo_world* w, const ribo_world_settings* s);
+ribo_status ribo_world_get_settings(const ribo_world* w, ribo_world_settings* out);
+
+// queue.write_buffer on a world buffer (seed_matter, src/world/mod.rs:969-988):
+// copies `bytes` (must equal the field size) from host memory.  Uploading
+// GAMMA recomputes the slope and the fluid wall mask.
+ribo_status ribo_world_upload(ribo_world* w, ribo_field field, const void* host, size_t bytes);
+
+// read_cells_blocking / read_f32_blocking (src/world/mod.rs:1801-1809):
+// waits for the world's stream, then copies the field to host memory.
+ribo_status ribo_world_read(ribo_world* w, ribo_field field, void* host, size_t bytes);
+
+// The device address and size of a field (for zero-copy callers on the same
+// device).  The pointer stays valid until ribo_world_destroy.
+ribo_status ribo_world_device_ptr(ribo_world* w, ribo_field field, void** dptr, size_t* bytes);
+
+// Records `n` steps (1..64) with explicit per-step parameters, asynchronously
+// on the world's stream: the dispatch sequence of World::encode_steps
+// (src/world/mod.rs:1487-1601) for the fluid and transport blocks.  The fluid
+// block runs when settings.fluid_enabled and epoch % fluid_substep == 0; the
+// transport block when epoch % transport_every == 0.
+ribo_status ribo_world_step(ribo_world* w, const ribo_sim_params* per_step, uint32_t n);
+
+// World::encode_steps (src/world/mod.rs:1406-1632): derives the per-step
+// copies from `params` (epoch + i, fluid_dt = dt * substep, fluid_enabled from
+// the settings, sun_now / sun_slope from the day cycle), records them, and
+// advances params->epoch by `steps` (at most 64 per call, as MAX_STEPS_PER_FRAME).
+ribo_status ribo_world_encode_steps(ribo_world* w, ribo_sim_params* params, uint32_t steps);
+
+// The per-step copies World::encode_steps would write for `steps` steps
+// starting at base->epoch (out must hold `steps` entries).
+ribo_status ribo_derive_step_params(const ribo_sim_params* base, const ribo_world_settings* settings,
+                                    uint32_t steps, ribo_sim_params* out);
+
+// ledger_blocking (src/world/mod.rs:1834-1839, shaders/world/ledger.wgsl):
+// exact per-channel sums [activated A U G C, spent A U G C, held A U G C]
+// (held is 0: no agents on this path).  Waits for the world's stream.
+ribo_status ribo_world_ledger(ribo_world* w, uint32_t out[12]);
+
+// With settings.ledger_each_step, the ledger of the state after each step of
+// the last ribo_world_step / encode_steps call (12 words per step, `n` steps
+// of that call).  Waits for the world's stream.
+ribo_status ribo_world_step_ledgers(ribo_world* w, uint32_t* out, uint32_t n);
+
+// Records timing mark `slot` (0..7) on the world's stream, and the device
+// time between two recorded marks in ms (waits for the second).
+ribo_status ribo_world_mark(ribo_world* w, uint32_t slot);
+ribo_status ribo_world_elapsed_ms(ribo_world* w, uint32_t slot_a, uint32_t slot_b, float* ms);
+
+// Waits until all work recorded on the world's stream has finished.
+ribo_status ribo_world_sync(ribo_world* w);
+
+// Device time of the last ribo_world_step / encode_steps call, in ms (CUDA
+// events on the world's stream; waits for it).
+ribo_status ribo_world_last_step_ms(ribo_world* w, float* ms);
+
+// Per-kernel GPU timing, the counterpart of World::enable_kernel_timing /
+// read_kernel_timing (src/world/mod.rs:1056-1098): when enabled, every
+// kernel of the following ribo_world_step / encode_steps call is bracketed
+// by CUDA events on the world's stream.  read_kernel_timing waits for the
+// stream and returns one entry per kernel name, summed over that call:
+// launches, milliseconds and the algorithmic bytes (compulsory reads +
+// writes) those launches move.
+typedef struct ribo_kernel_timing {
+  char name[40];
+  uint32_t launches;
+  float ms;
+  double bytes;
+} ribo_kernel_timing;
+ribo_status ribo_world_enable_kernel_timing(ribo_world* w, int enable);
+ribo_status ribo_world_read_kernel_timing(ribo_world* w, ribo_kernel_timing* out, uint32_t cap, uint32_t* count);
+
+// Number of kernels this library has launched in this process so far.
+uint64_t ribo_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}  // extern "C"
+#endif

@@ -1,0 +1,445 @@
+// Fluid passes of the world step (stable fluids at fluid resolution).
+// Each kernel restates one WGSL entry point of shaders/world/fluid.wgsl,
+// one thread per fluid cell, with the same float operation order.
+#include "ribo_dev.cuh"
+#include "ribo_launch.h"
+
+namespace ribo {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+inline dim3 grid2(int w, int h) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY); }
+
+// fluid.wgsl:95-109,138-142,185-189
+__global__ void k_solid_mask(const __grid_constant__ Dev d) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  float gx = ((float)x + 0.5f) * d.sx, gy = ((float)y + 0.5f) * d.sy;
+  float hx = d.sx * 0.25f, hy = d.sy * 0.25f;
+  uint32_t n_solid = 0;
+#pragma unroll
+  for (uint32_t s = 0; s < 4; s++) {
+    float ox = (s & 1u) == 1u ? hx : -hx;
+    float oy = (s & 2u) == 2u ? hy : -hy;
+    uint32_t sx = rb_f2u(rb_clamp(gx + ox, 0.0f, (float)(d.gw - 1)));
+    uint32_t sy = rb_f2u(rb_clamp(gy + oy, 0.0f, (float)(d.gh - 1)));
+    if (__ldg(d.gamma + (size_t)sy * d.gw + sx) >= GAMMA_SOLID) n_solid++;
+  }
+  float solidity = (float)n_solid * 0.25f;
+  float perm = solidity >= 0.5f ? 0.0f : rb_clamp(1.0f - solidity * 2.0f, 0.0f, 1.0f);
+  d.mask[(size_t)y * d.fw + x] = perm < SOLID_PERM_THRESHOLD ? 1 : 0;
+}
+
+// fluid.wgsl:300-372 (update_temperature; copy_temperature becomes a
+// pointer swap on the host, and the redox_eaten reset happens here after
+// its single read).
+__global__ void k_temperature(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  const int fw = d.fw, fh = d.fh;
+  size_t idx = (size_t)y * fw + x;
+  const float dt = fluid_dt(P);
+  float2 vel = raw_velocity_cell(d, d.va, x, y);
+  float srcx = ((float)x + 0.5f) - vel.x * dt;
+  float srcy = ((float)y + 0.5f) - vel.y * dt;
+  float sxf = rb_clamp(srcx - 0.5f, 0.0f, (float)(fw - 1));
+  float syf = rb_clamp(srcy - 0.5f, 0.0f, (float)(fh - 1));
+  uint32_t x0 = rb_f2u(rb_floor(sxf)), y0 = rb_f2u(rb_floor(syf));
+  uint32_t x1 = umin(x0 + 1u, (uint32_t)fw - 1u), y1 = umin(y0 + 1u, (uint32_t)fh - 1u);
+  float fx = rb_fract(sxf), fy = rb_fract(syf);
+  const float* T = d.temp_in;
+  float t = rb_mix(rb_mix(T[(size_t)y0 * fw + x0], T[(size_t)y0 * fw + x1], fx),
+                   rb_mix(T[(size_t)y1 * fw + x0], T[(size_t)y1 * fw + x1], fx), fy);
+  uint32_t xl = x > 0u ? x - 1u : 0u, xr = umin(x + 1u, (uint32_t)fw - 1u);
+  uint32_t yb = y > 0u ? y - 1u : 0u, yt = umin(y + 1u, (uint32_t)fh - 1u);
+  float tl = T[(size_t)y * fw + xl], tr = T[(size_t)y * fw + xr], tb = T[(size_t)yb * fw + x], tt = T[(size_t)yt * fw + x];
+  float fill = gamma_fill_at_fluid_cell(d, x, y);
+  t = rb_mix(t, (tl + tr + tb + tt) * 0.25f, TEMP_DIFFUSE * rb_mix(1.0f, TEMP_ROCK_CONDUCT, fill));
+  float vc = vent_cycle(d, P, x);
+  float2 h = d.heat[idx];
+  t += h.x * vc * TEMP_HEAT_RATE * dt;
+  if (rb_max(P->sun_heat, 0.0f) > 0.0f) {  // otherwise the sun term is exactly 0
+    size_t env = env_cell_for_fluid(d, x, y);
+    float depth = 1.0f - ((float)y + 0.5f) / (float)fh;
+    float ir = P->sun_now * SUN_IR * rb_exp(-depth / SUN_IR_DEPTH);
+    t += rb_max(P->sun_heat, 0.0f) * SUN_HEAT_RATE * (light_absorbed_at(d, P, env) + ir) * dt;
+  }
+  float amb = temp_ambient_at(d, y);
+  t = amb + (t - amb) * rb_exp(-TEMP_COOL_RATE * (1.0f - fill) * dt);
+  d.temp_out[idx] = rb_clamp(t, 0.0f, TEMP_MAX);
+
+  const float* R = d.redox_in;
+  float r = rb_mix(rb_mix(R[(size_t)y0 * fw + x0], R[(size_t)y0 * fw + x1], fx),
+                   rb_mix(R[(size_t)y1 * fw + x0], R[(size_t)y1 * fw + x1], fx), fy);
+  float rl = R[(size_t)y * fw + xl], rr = R[(size_t)y * fw + xr], rbt = R[(size_t)yb * fw + x], rt = R[(size_t)yt * fw + x];
+  r = rb_mix(r, (rl + rr + rbt + rt) * 0.25f, TEMP_DIFFUSE);
+  r += h.y * vc * REDOX_RATE * dt;
+  r = rb_max(r - (float)d.redox_eaten[idx] / REDOX_FP, 0.0f);
+  r *= rb_exp(-rb_max(P->redox_decay, 0.0f) * dt);
+  d.redox_out[idx] = rb_clamp(r, 0.0f, REDOX_MAX);
+  d.redox_eaten[idx] = 0u;
+}
+
+// fluid.wgsl:280-296,376-404: buoyancy adds into the fixed-point force
+// accumulators (each interior cell writes only its own slots, so the add
+// needs no atomics), gather_forces converts and clamps them, and
+// clear_force_vectors zeroes them -- all in one pass.
+__device__ __forceinline__ uint32_t quant_force(float v) {
+  int32_t q = rb_f2i(rb_rint(rb_clamp(v, (float)-1.0e5, (float)1.0e5) * FORCE_FP));
+  return (uint32_t)q;
+}
+__global__ void k_forces(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  size_t idx = (size_t)y * d.fw + x;
+  uint2 fv = reinterpret_cast<uint2*>(d.force_vec)[idx];
+  if (!(x == 0u || y == 0u || x >= (uint32_t)d.fw - 1u || y >= (uint32_t)d.fh - 1u)) {
+    float dev = d.temp_in[idx] - temp_ambient_at(d, y);
+    if (!(rb_abs(dev) <= (float)1e-3)) {
+      uint32_t time_bucket = P->epoch / 16u;
+      float r = rb_u2f(rb_pcg4d((uint32_t)idx, time_bucket, RB_S_BUOYANCY, P->seed).x);
+      float side = (r * 2.0f - 1.0f) * 0.25f * rb_abs(dev) / rb_max(rb_abs(dev), 1.0f);
+      fv.x += quant_force(side * TEMP_BUOYANCY * rb_abs(dev));
+      fv.y += quant_force(TEMP_BUOYANCY * dev);
+    }
+  }
+  float2 f = f2((float)(int32_t)fv.x / FORCE_FP, (float)(int32_t)fv.y / FORCE_FP);
+  d.forces[idx] = clamp_len(sanitize(f), MAX_FORCE);
+  reinterpret_cast<uint2*>(d.force_vec)[idx] = make_uint2(0u, 0u);
+}
+
+// fluid.wgsl:150-161
+__device__ __forceinline__ float rubble_drag(const Dev& d, uint32_t x, uint32_t y, float dt) {
+  float g = 0.0f;
+  for (int dy = 0; dy < d.ry; dy++)
+    for (int dx = 0; dx < d.rx; dx++) {
+      uint32_t c = __ldg(d.gamma + (size_t)(y * d.ry + dy) * d.gw + x * d.rx + dx);
+      if (c < GAMMA_SOLID) g += (float)c;
+    }
+  g = g / ((float)(d.rx * d.ry) * (float)GAMMA_SOLID);
+  return 1.0f / (1.0f + RUBBLE_DRAG * g * dt);
+}
+// fluid.wgsl:165-178
+__device__ __forceinline__ float2 slope_steer(const Dev& d, const ribo_sim_params* P, uint32_t x, uint32_t y, float2 v_in, float dt) {
+  float2 s0 = sanitize(d.slope[env_cell_for_fluid(d, x, y)]);
+  float2 s = f2(-s0.x, -s0.y);
+  float v_len = len2(v_in), s_len = len2(s);
+  if (v_len < (float)1e-5 || s_len < (float)1e-5) return v_in;
+  float2 v_dir = div2(v_in, v_len), s_dir = div2(s, s_len);
+  float misalign = rb_clamp(1.0f - dot2(v_dir, s_dir), 0.0f, 2.0f);
+  float t = rb_clamp(1.0f - rb_exp(-rb_max(P->slope_steer_rate, 0.0f) * misalign * dt), 0.0f, 1.0f);
+  float2 dir_raw = add2(v_dir, mul2(sub2(s_dir, v_dir), t));
+  float dir_len = len2(dir_raw);
+  if (dir_len < (float)1e-5) return v_in;
+  return mul2(div2(dir_raw, dir_len), v_len);
+}
+
+// fluid.wgsl:410-432 (add_forces; clear_forces is dropped: gather
+// overwrites every fluid_forces entry before the next read)
+__global__ void k_add_forces(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
+                             float2* __restrict__ vout) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  const int fw = d.fw;
+  size_t idx = (size_t)y * fw + x;
+  if (is_solid(d, x, y)) {
+    vout[idx] = f2(0.0f, 0.0f);
+    return;
+  }
+  const float dt = fluid_dt(P);
+  uint32_t xm = x > 0u ? x - 1u : x, xp = x + 1u < (uint32_t)fw ? x + 1u : x;
+  uint32_t ym = y > 0u ? y - 1u : y, yp = y + 1u < (uint32_t)d.fh ? y + 1u : y;
+  auto F = [&](uint32_t a, uint32_t b) { return sanitize(d.forces[(size_t)b * fw + a]); };
+  float2 f_c = F(x, y);
+  float2 axis = add2(add2(add2(F(xm, y), F(xp, y)), F(x, ym)), F(x, yp));
+  float2 diag = add2(add2(add2(F(xm, ym), F(xp, ym)), F(xm, yp)), F(xp, yp));
+  float2 f_avg = mul2(add2(add2(smul2(4.0f, axis), diag), smul2(20.0f, f_c)), (float)(1.0 / 36.0));
+  float2 f_user = clamp_len(mix2(f_c, f_avg, FORCE_SMOOTH_MIX), MAX_FORCE);
+  float2 v = sanitize(add2(sanitize(vin[idx]), mul2(f_user, dt)));
+  v = slope_steer(d, P, x, y, v, dt);
+  v = mul2(v, rubble_drag(d, x, y, dt));
+  v = reflect_if_into_solid(d, x, y, v);
+  vout[idx] = clamp_len(v, MAX_VEL);
+}
+
+// fluid.wgsl:435-456
+__global__ void k_diffuse(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
+                          float2* __restrict__ vout) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  size_t idx = (size_t)y * d.fw + x;
+  if (is_solid(d, x, y)) {
+    vout[idx] = f2(0.0f, 0.0f);
+    return;
+  }
+  if (x == 0u || x == (uint32_t)d.fw - 1u || y == 0u || y == (uint32_t)d.fh - 1u) {
+    vout[idx] = vin[idx];
+    return;
+  }
+  float2 v_c = raw_velocity_cell(d, vin, x, y);
+  float2 axis_sum = add2(add2(add2(raw_velocity_cell(d, vin, x - 1, y), raw_velocity_cell(d, vin, x + 1, y)),
+                              raw_velocity_cell(d, vin, x, y - 1)),
+                         raw_velocity_cell(d, vin, x, y + 1));
+  float2 diag_sum = add2(add2(add2(raw_velocity_cell(d, vin, x - 1, y - 1), raw_velocity_cell(d, vin, x + 1, y - 1)),
+                              raw_velocity_cell(d, vin, x - 1, y + 1)),
+                         raw_velocity_cell(d, vin, x + 1, y + 1));
+  float2 lap = mul2(sub2(add2(smul2(4.0f, axis_sum), diag_sum), smul2(20.0f, v_c)), (float)(1.0 / 6.0));
+  float a = rb_max(P->fluid_viscosity, 0.0f) * fluid_dt(P);
+  float2 v = sanitize(add2(v_c, smul2(a, lap)));
+  v = reflect_if_into_solid(d, x, y, v);
+  vout[idx] = clamp_len(v, MAX_VEL);
+}
+
+// fluid.wgsl:226-255
+__device__ __forceinline__ bool is_solid_at_pos(const Dev& d, float2 pos) {
+  int ix = rb_f2i(rb_floor(pos.x - 0.5f));
+  int iy = rb_f2i(rb_floor(pos.y - 0.5f));
+  if (ix < 0 || ix >= d.fw || iy < 0 || iy >= d.fh) return true;
+  return is_solid(d, ix, iy);
+}
+__device__ __forceinline__ float2 sample_velocity(const Dev& d, const float2* vin, float2 pos) {
+  float max_x = (float)d.fw - 0.5f, max_y = (float)d.fh - 0.5f;
+  if (pos.x < 0.5f || pos.x > max_x || pos.y < 0.5f || pos.y > max_y) return f2(0.0f, 0.0f);
+  float x = pos.x - 0.5f, y = pos.y - 0.5f;
+  int x0 = rb_f2i(rb_floor(x)), y0 = rb_f2i(rb_floor(y));
+  float fx = rb_fract(x), fy = rb_fract(y);
+  uint32_t cx0 = iclamp(x0, 0, d.fw - 1), cx1 = iclamp(x0 + 1, 0, d.fw - 1);
+  uint32_t cy0 = iclamp(y0, 0, d.fh - 1), cy1 = iclamp(y0 + 1, 0, d.fh - 1);
+  float2 v0 = mix2(raw_velocity_cell(d, vin, cx0, cy0), raw_velocity_cell(d, vin, cx1, cy0), fx);
+  float2 v1 = mix2(raw_velocity_cell(d, vin, cx0, cy1), raw_velocity_cell(d, vin, cx1, cy1), fx);
+  return mix2(v0, v1, fy);
+}
+// fluid.wgsl:458-477
+__global__ void k_advect(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
+                         float2* __restrict__ vout) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  size_t idx = (size_t)y * d.fw + x;
+  if (is_solid(d, x, y)) {
+    vout[idx] = f2(0.0f, 0.0f);
+    return;
+  }
+  const float dt = fluid_dt(P);
+  const float decay_factor = rb_pow(rb_clamp(P->fluid_decay, 0.0f, 1.0f), dt * 60.0f);
+  float2 n = solid_normal(d, x, y);
+  float2 pos = f2((float)x + 0.5f, (float)y + 0.5f);
+  float2 vel = reflect_n(n, clamp_len(raw_velocity_cell(d, vin, x, y), MAX_VEL));
+  float2 trace_pos = sub2(pos, mul2(vel, dt));
+  if (is_solid_at_pos(d, trace_pos)) trace_pos = sub2(pos, mul2(reflect_n(n, vel), dt));
+  float2 out_v = sanitize(mul2(sample_velocity(d, vin, trace_pos), decay_factor));
+  out_v = reflect_n(n, out_v);
+  vout[idx] = clamp_len(out_v, MAX_VEL);
+}
+
+// fluid.wgsl:479-518
+__device__ __forceinline__ float curl_at(const Dev& d, const float2* vin, uint32_t x, uint32_t y) {
+  uint32_t xm = iclamp((int)x - 1, 0, d.fw - 1), xp = iclamp((int)x + 1, 0, d.fw - 1);
+  uint32_t ym = iclamp((int)y - 1, 0, d.fh - 1), yp = iclamp((int)y + 1, 0, d.fh - 1);
+  float2 v_l = reflect_if_into_solid(d, xm, y, raw_velocity_cell(d, vin, xm, y));
+  float2 v_r = reflect_if_into_solid(d, xp, y, raw_velocity_cell(d, vin, xp, y));
+  float2 v_b = reflect_if_into_solid(d, x, ym, raw_velocity_cell(d, vin, x, ym));
+  float2 v_t = reflect_if_into_solid(d, x, yp, raw_velocity_cell(d, vin, x, yp));
+  return 0.5f * (v_r.y - v_l.y) - 0.5f * (v_t.x - v_b.x);
+}
+__global__ void k_vorticity(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
+                            float2* __restrict__ vout) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  size_t idx = (size_t)y * d.fw + x;
+  if (is_solid(d, x, y)) {
+    vout[idx] = f2(0.0f, 0.0f);
+    return;
+  }
+  const float epsilon = rb_clamp(P->fluid_vorticity, 0.0f, 10.0f);
+  const uint32_t border = 2u;
+  if (x < border || x >= (uint32_t)d.fw - border || y < border || y >= (uint32_t)d.fh - border || epsilon < (float)1e-6) {
+    vout[idx] = vin[idx];
+    return;
+  }
+  float w = curl_at(d, vin, x, y);
+  if (rb_abs(w) < (float)5e-4) {
+    vout[idx] = vin[idx];
+    return;
+  }
+  float2 grad = mul2(f2(rb_abs(curl_at(d, vin, x + 1, y)) - rb_abs(curl_at(d, vin, x - 1, y)),
+                        rb_abs(curl_at(d, vin, x, y + 1)) - rb_abs(curl_at(d, vin, x, y - 1))),
+                     0.5f);
+  float2 n = div2(grad, rb_max(len2(grad), (float)1e-5));
+  float2 f = mul2(f2(n.y, -n.x), w * epsilon);
+  float2 dv = clamp_len(mul2(f, fluid_dt(P)), 2.0f);
+  float2 v = sanitize(add2(vin[idx], dv));
+  v = reflect_if_into_solid(d, x, y, v);
+  vout[idx] = clamp_len(v, MAX_VEL);
+}
+
+// fluid.wgsl:520-551
+__device__ __forceinline__ float2 div_neighbor(const Dev& d, const float2* vin, float2 v_c, int nx, int ny, bool axis_x) {
+  bool outside = nx < 0 || ny < 0 || nx >= d.fw || ny >= d.fh;
+  if (outside || is_solid(d, nx, ny)) return axis_x ? f2(-v_c.x, v_c.y) : f2(v_c.x, -v_c.y);
+  return raw_velocity_cell(d, vin, nx, ny);
+}
+__global__ void k_divergence(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
+  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= d.fw || y >= d.fh) return;
+  size_t idx = (size_t)y * d.fw + x;
+  if (is_solid(d, x, y)) {
+    d.div[idx] = 0.0f;
+    return;
+  }
+  float2 v_c = raw_velocity_cell(d, vin, x, y);
+  float2 v_l = div_neighbor(d, vin, v_c, x - 1, y, true);
+  float2 v_r = div_neighbor(d, vin, v_c, x + 1, y, true);
+  float2 v_b = div_neighbor(d, vin, v_c, x, y - 1, false);
+  float2 v_t = div_neighbor(d, vin, v_c, x, y + 1, false);
+  d.div[idx] = 0.5f * ((v_r.x - v_l.x) + (v_t.y - v_b.y));
+}
+
+// fluid.wgsl:610-630
+__global__ void k_subtract_gradient(const __grid_constant__ Dev d, const float2* __restrict__ vin, float2* __restrict__ vout) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  const int fw = d.fw;
+  size_t idx = (size_t)y * fw + x;
+  if (is_solid(d, x, y)) {
+    vout[idx] = f2(0.0f, 0.0f);
+    return;
+  }
+  const float* p = d.pa;
+  float p_c = p[idx];
+  float p_l = p_c, p_r = p_c, p_b = p_c, p_t = p_c;
+  if (x > 0u && !is_solid(d, x - 1, y)) p_l = p[idx - 1];
+  if (x + 1u < (uint32_t)fw && !is_solid(d, x + 1, y)) p_r = p[idx + 1];
+  if (y > 0u && !is_solid(d, x, y - 1)) p_b = p[idx - fw];
+  if (y + 1u < (uint32_t)d.fh && !is_solid(d, x, y + 1)) p_t = p[idx + fw];
+  float2 grad = mul2(f2(p_r - p_l, p_t - p_b), 0.5f);
+  float2 v = sub2(sanitize(vin[idx]), grad);
+  v = reflect_if_into_solid(d, x, y, v);
+  vout[idx] = clamp_len(sanitize(v), MAX_VEL);
+}
+
+// fluid.wgsl:640-657.  The reference sums each row (column) serially in
+// f32; the order of those adds fixes the rounding, so each line is summed
+// by one thread in index order.  Rows are staged through shared memory in
+// 32x32 tiles so the loads stay coalesced.
+constexpr int NF_LINES = 32;
+__global__ void k_net_flux_rows(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
+  __shared__ float tile[NF_LINES][33];
+  __shared__ uint8_t stile[NF_LINES][33];
+  int row0 = blockIdx.x * NF_LINES;
+  int lane = threadIdx.x;  // 32 threads
+  float sum = 0.0f, n = 0.0f;
+  int my_row = row0 + lane;
+  for (int x0 = 0; x0 < d.fw; x0 += 32) {
+    for (int r = 0; r < NF_LINES; r++) {
+      int yy = row0 + r, xx = x0 + lane;
+      float v = 0.0f;
+      uint8_t s = 1;
+      if (yy < d.fh && xx < d.fw) {
+        size_t i = (size_t)yy * d.fw + xx;
+        s = d.mask[i];
+        v = sanitize(vin[i]).y;
+      }
+      tile[r][lane] = v;
+      stile[r][lane] = s;
+    }
+    __syncwarp();
+    int lim = min(32, d.fw - x0);
+    for (int k = 0; k < lim; k++) {
+      if (stile[lane][k]) continue;
+      sum += tile[lane][k];
+      n += 1.0f;
+    }
+    __syncwarp();
+  }
+  if (my_row < d.fh) d.net_flux[my_row] = n > 0.0f ? sum / n : 0.0f;
+}
+__global__ void k_net_flux_cols(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
+  int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.fw) return;
+  float sum = 0.0f, n = 0.0f;
+  for (int k = 0; k < d.fh; k++) {
+    size_t i = (size_t)k * d.fw + col;
+    if (d.mask[i]) continue;
+    sum += sanitize(vin[i]).x;
+    n += 1.0f;
+  }
+  d.net_flux[d.fh + col] = n > 0.0f ? sum / n : 0.0f;
+}
+
+// fluid.wgsl:663-677
+__global__ void k_boundaries(const __grid_constant__ Dev d, const float2* __restrict__ vin, float2* __restrict__ vout) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  size_t idx = (size_t)y * d.fw + x;
+  if (is_solid(d, x, y)) {
+    vout[idx] = f2(0.0f, 0.0f);
+    return;
+  }
+  float2 v = sanitize(vin[idx]);
+  v = sub2(v, f2(d.net_flux[d.fh + x], d.net_flux[y]));
+  if (x == 0u || x == (uint32_t)d.fw - 1u) v.x = 0.0f;
+  if (y == 0u || y == (uint32_t)d.fh - 1u) v.y = 0.0f;
+  v = reflect_if_into_solid(d, x, y, v);
+  vout[idx] = clamp_len(sanitize(v), MAX_VEL);
+}
+
+// fluid.wgsl:680-693
+__global__ void k_smooth(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  const int fw = d.fw;
+  uint32_t xm = x > 0u ? x - 1u : x, xp = umin(x + 1u, (uint32_t)fw - 1u);
+  uint32_t ym = y > 0u ? y - 1u : y, yp = umin(y + 1u, (uint32_t)d.fh - 1u);
+  float2 v = add2(add2(add2(add2(sanitize(vin[(size_t)y * fw + x]), sanitize(vin[(size_t)y * fw + xm])),
+                             sanitize(vin[(size_t)y * fw + xp])),
+                        sanitize(vin[(size_t)ym * fw + x])),
+                   sanitize(vin[(size_t)yp * fw + x]));
+  d.vsmooth[(size_t)y * fw + x] = mul2(v, 0.2f);
+}
+
+}  // namespace
+
+inline double fc(const Dev& d) { return (double)d.fw * d.fh; }
+inline double gc(const Dev& d) { return (double)d.gw * d.gh; }
+
+void launch_solid_mask(const Dev& d, cudaStream_t s) {
+  RB_LAUNCH("build_solid_mask", 4.0 * gc(d) + fc(d), s, k_solid_mask<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d));
+}
+void launch_temperature(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
+  RB_LAUNCH("update_temperature", 41.0 * fc(d) + 4.0 * gc(d), s, k_temperature<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P));
+}
+void launch_forces(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
+  RB_LAUNCH("forces", 28.0 * fc(d), s, k_forces<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P));
+}
+void launch_add_forces(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
+  RB_LAUNCH("add_forces", 33.0 * fc(d) + 4.0 * gc(d), s, k_add_forces<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+}
+void launch_diffuse(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
+  RB_LAUNCH("diffuse_velocity", 17.0 * fc(d), s, k_diffuse<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+}
+void launch_advect(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
+  RB_LAUNCH("advect_velocity", 17.0 * fc(d), s, k_advect<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+}
+void launch_vorticity(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
+  RB_LAUNCH("vorticity", 17.0 * fc(d), s, k_vorticity<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+}
+void launch_divergence(const Dev& d, const float2* vin, cudaStream_t s) {
+  RB_LAUNCH("divergence", 13.0 * fc(d), s, k_divergence<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin));
+}
+void launch_subtract_gradient(const Dev& d, const float2* vin, float2* vout, cudaStream_t s) {
+  RB_LAUNCH("subtract_gradient", 21.0 * fc(d), s, k_subtract_gradient<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin, vout));
+}
+void launch_net_flux(const Dev& d, const float2* vin, cudaStream_t s) {
+  RB_LAUNCH("net_flux_rows", 9.0 * fc(d), s, k_net_flux_rows<<<(d.fh + NF_LINES - 1) / NF_LINES, 32, 0, s>>>(d, vin));
+  RB_LAUNCH("net_flux_cols", 9.0 * fc(d), s, k_net_flux_cols<<<(d.fw + 63) / 64, 64, 0, s>>>(d, vin));
+}
+void launch_boundaries(const Dev& d, const float2* vin, float2* vout, cudaStream_t s) {
+  RB_LAUNCH("enforce_boundaries", 17.0 * fc(d), s, k_boundaries<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin, vout));
+}
+void launch_smooth(const Dev& d, const float2* vin, cudaStream_t s) {
+  RB_LAUNCH("smooth_velocity", 16.0 * fc(d), s, k_smooth<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin));
+}
+
+}  // namespace ribo

@@ -1,0 +1,96 @@
+// The World object behind the C handle (host side; see world.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ribo_world.h"
+#include "ribo_dev.cuh"
+#include "ribo_launch.h"
+
+namespace ribo {
+
+ribo_status set_error(ribo_status st, const char* fmt, ...);
+ribo_status cuda_status(cudaError_t e, const char* what);
+
+// Events bracketing each kernel launch of one step call (kernel timing).
+struct KTimer {
+  struct Rec {
+    const char* label;
+    double bytes;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  std::vector<Rec> recs;
+  cudaEvent_t event();
+  ~KTimer();
+};
+
+struct World {
+  ribo_world_cfg cfg{};
+  ribo_world_settings st{};
+  int gw = 0, gh = 0, fw = 0, fh = 0;
+  bool fluid_was_on = true;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  std::vector<void*> allocs;
+
+  // environment resolution
+  uint32_t *chem_a = nullptr, *chem_b = nullptr, *chem_cur = nullptr, *chem_nxt = nullptr;
+  uint32_t* gamma = nullptr;
+  float* light = nullptr;
+  uint32_t* shade = nullptr;
+  float2* slope = nullptr;
+  uint32_t *agg_act = nullptr, *agg_nb = nullptr;
+  // fluid resolution
+  uint8_t* mask = nullptr;
+  uint32_t* mask32 = nullptr;
+  float2 *va = nullptr, *vb = nullptr, *vsmooth = nullptr;
+  float *pa = nullptr, *pb = nullptr, *div = nullptr;
+  float *temp_a = nullptr, *temp_b = nullptr, *temp_cur = nullptr, *temp_nxt = nullptr;
+  float *redox_a = nullptr, *redox_b = nullptr, *redox_cur = nullptr, *redox_nxt = nullptr;
+  uint32_t* redox_eaten = nullptr;
+  uint32_t* force_vec = nullptr;
+  float2* forces = nullptr;
+  float2* heat = nullptr;
+  float* net_flux = nullptr;
+  uint32_t* ledger = nullptr;
+  uint32_t* step_ledgers = nullptr;  // 64 x 12 words (ledger_each_step)
+  uint32_t last_steps = 0;
+  // multigrid
+  std::vector<MgLevel> levels;
+  size_t mg_total = 0;
+  MgBufs mg{};
+  // per-step parameters: two slots of 64 copies, device + pinned staging
+  ribo_sim_params* d_params = nullptr;
+  ribo_sim_params* h_params = nullptr;
+  cudaEvent_t param_ev[2] = {nullptr, nullptr};
+  int param_slot = 0;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  cudaEvent_t marks[8] = {};
+  bool timing = false;
+  KTimer timer;
+
+  size_t cells() const { return (size_t)gw * gh; }
+  size_t fcells() const { return (size_t)fw * fh; }
+  size_t lcells() const { return (size_t)(gw / 2) * (gh / 2); }
+  size_t field_bytes(ribo_field f) const;
+  void* field_ptr(ribo_field f);
+  Dev dev() const;
+
+  ribo_status alloc(void** p, size_t bytes, const char* what);
+  ribo_status init(const ribo_world_cfg& c);
+  ~World();
+  ribo_status upload(ribo_field f, const void* host, size_t bytes);
+  ribo_status read(ribo_field f, void* host, size_t bytes);
+  ribo_status step(const ribo_sim_params* per_step, uint32_t n);
+  ribo_status ledger_read(uint32_t out[12]);
+  ribo_status read_timing(ribo_kernel_timing* out, uint32_t cap, uint32_t* count);
+  void record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uint32_t i);
+  cudaError_t bind() const;
+  void pressure_solve(const Dev& d);
+};
+
+}  // namespace ribo

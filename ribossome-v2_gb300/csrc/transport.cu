@@ -1,0 +1,363 @@
+// Monomer transport and reactions, ledger and terrain slope
+// (shaders/world/transport.wgsl, ledger.wgsl, terrain.wgsl:104-133).
+//
+// Transport is a two-phase scatter: every cell reads the state before the
+// step (chem) and adds each monomer to exactly one destination word of
+// chem_next with integer atomics.  Integer adds commute, so the result is
+// independent of thread order and bit-identical to the oracle.
+#include "ribo_dev.cuh"
+#include "ribo_launch.h"
+
+namespace ribo {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+inline dim3 grid2(int w, int h) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY); }
+
+// terrain.wgsl:104-133 (compute_gamma_slope)
+__global__ void k_slope(const __grid_constant__ Dev d, float upc) {
+  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= d.gw || y >= d.gh) return;
+  auto h = [&](int ix, int iy) {
+    int cx = iclamp(ix, 0, d.gw - 1), cy = iclamp(iy, 0, d.gh - 1);
+    return (float)__ldg(d.gamma + (size_t)cy * d.gw + cx) * GAMMA_QUANTUM;
+  };
+  float l = h(x - 1, y), r = h(x + 1, y), b = h(x, y - 1), t = h(x, y + 1);
+  float bl = h(x - 1, y - 1), br = h(x + 1, y - 1), tl = h(x - 1, y + 1), tr = h(x + 1, y + 1);
+  const float k = (float)(1.0 / (4.0 * 1.41421356237));
+  float dx = (r - l) * 0.5f + (tr + br - tl - bl) * k;
+  float dy = (t - b) * 0.5f + (tl + tr - bl - br) * k;
+  d.slope[(size_t)y * d.gw + x] = f2(dx / upc, dy / upc);
+}
+
+// transport.wgsl:419-438 (thermal activation, in place; one thread per cell)
+__global__ void k_thermal(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.gw || y >= (uint32_t)d.gh) return;
+  uint32_t fx = umin((x * (uint32_t)d.fw) / (uint32_t)d.gw, (uint32_t)d.fw - 1u);
+  uint32_t fy = umin((y * (uint32_t)d.fh) / (uint32_t)d.gh, (uint32_t)d.fh - 1u);
+  float t_loc = d.temp_in[(size_t)fy * d.fw + fx];
+  if (t_loc <= TEMP_ACT_THRESHOLD) return;
+  float p_act = rb_clamp(FUMAROLE_ACT_P * rb_max(P->thermal_activation, 0.0f) * (t_loc - TEMP_ACT_THRESHOLD) / TEMP_ACT_THRESHOLD, 0.0f,
+                         (float)0.9);
+  size_t idx = (size_t)y * d.gw + x;
+  uint4 c = reinterpret_cast<uint4*>(d.chem)[idx];
+  uint32_t w[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+  for (uint32_t ch = 0; ch < 4; ch++) {
+    uint32_t slot = (uint32_t)(idx * 4 + ch);
+    if ((w[ch] >> 16) > 0u && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_THERMAL, P->seed).x) < p_act) w[ch] += 0xFFFF0001u;
+  }
+  reinterpret_cast<uint4*>(d.chem)[idx] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// transport.wgsl:61-68
+__global__ void k_agg_count(const __grid_constant__ Dev d) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)d.gw * d.gh) return;
+  uint4 c = load_cell(d.chem, i);
+  d.agg_act[i] = (c.x & CHEM_STATE_MASK) + (c.y & CHEM_STATE_MASK) + (c.z & CHEM_STATE_MASK) + (c.w & CHEM_STATE_MASK);
+}
+// transport.wgsl:71-87
+__global__ void k_agg_neighbours(const __grid_constant__ Dev d) {
+  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= d.gw || y >= d.gh) return;
+  uint32_t sum = 0;
+  for (int dy = -1; dy <= 1; dy++)
+    for (int dx = -1; dx <= 1; dx++) {
+      if (dx == 0 && dy == 0) continue;
+      int nx = x + dx, ny = y + dy;
+      if (nx < 0 || ny < 0 || nx >= d.gw || ny >= d.gh) continue;
+      sum += d.agg_act[(size_t)ny * d.gw + nx];
+    }
+  d.agg_nb[(size_t)y * d.gw + x] = sum;
+}
+
+// transport.wgsl:260-273 (fluid_velocity_at_world, reading velocity_a)
+__device__ __forceinline__ float2 fluid_velocity_at_world(const Dev& d, float2 pw) {
+  float gxf = (float)d.fw, gyf = (float)d.fh;
+  float gx = rb_clamp(pw.x / d.sim_w * gxf, 0.5f, gxf - 0.5f) - 0.5f;
+  float gy = rb_clamp(pw.y / d.sim_h * gyf, 0.5f, gyf - 0.5f) - 0.5f;
+  uint32_t x0 = rb_f2u(rb_floor(gx)), y0 = rb_f2u(rb_floor(gy));
+  uint32_t x1 = umin(x0 + 1u, (uint32_t)d.fw - 1u), y1 = umin(y0 + 1u, (uint32_t)d.fh - 1u);
+  float tx = rb_fract(gx), ty = rb_fract(gy);
+  const float2* v = d.va;
+  float2 v0 = mix2(sanitize(v[(size_t)y0 * d.fw + x0]), sanitize(v[(size_t)y0 * d.fw + x1]), tx);
+  float2 v1 = mix2(sanitize(v[(size_t)y1 * d.fw + x0]), sanitize(v[(size_t)y1 * d.fw + x1]), tx);
+  return mix2(v0, v1, ty);
+}
+
+// transport.wgsl:95-117
+__device__ __forceinline__ float2 lattice_rand(uint32_t ix, uint32_t iy, const ribo_sim_params* P) {
+  rb_u4 r = rb_pcg4d((ix * 73856093u) ^ (iy * 19349663u), P->epoch, RB_S_MOVE + MAX_MOVERS_PER_CH + 1u, P->seed);
+  return f2(rb_u2f(r.x), rb_u2f(r.y));
+}
+__device__ __forceinline__ float2 smooth_start(uint32_t x0, uint32_t y0, const ribo_sim_params* P) {
+  rb_u4 j = rb_pcg4d(0x85EBCA6Bu, P->epoch, RB_S_MOVE + MAX_MOVERS_PER_CH + 2u, P->seed);
+  uint32_t x = x0 + rb_f2u(rb_u2f(j.x) * (float)SMOOTH_CELL);
+  uint32_t y = y0 + rb_f2u(rb_u2f(j.y) * (float)SMOOTH_CELL);
+  uint32_t gx = x / SMOOTH_CELL, gy = y / SMOOTH_CELL;
+  float tx = rb_smoothstep01(((float)(x % SMOOTH_CELL) + 0.5f) / (float)SMOOTH_CELL);
+  float ty = rb_smoothstep01(((float)(y % SMOOTH_CELL) + 0.5f) / (float)SMOOTH_CELL);
+  float2 n = mix2(mix2(lattice_rand(gx, gy, P), lattice_rand(gx + 1u, gy, P), tx),
+                  mix2(lattice_rand(gx, gy + 1u, P), lattice_rand(gx + 1u, gy + 1u, P), tx), ty);
+  rb_u4 gr = rb_pcg4d(0x9E3779B9u, P->epoch, RB_S_MOVE + MAX_MOVERS_PER_CH, P->seed);
+  float vx = rb_fract(n.x + rb_u2f(gr.x)), vy = rb_fract(n.y + rb_u2f(gr.y));
+  return f2(1.0f - rb_abs(2.0f * vx - 1.0f), 1.0f - rb_abs(2.0f * vy - 1.0f));
+}
+
+// transport.wgsl:119-406
+__global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  const uint32_t G = d.gw, GH = d.gh;
+  if (x >= G || y >= GH) return;
+  size_t idx = (size_t)y * G + x;
+  uint4 cw = load_cell(d.chem, idx);
+  uint32_t src_total = cell_total4(cw);
+  if (src_total == 0u) return;
+  uint32_t g_src = __ldg(d.gamma + idx);
+  float2 v = f2(0.0f, 0.0f);
+  if (P->fluid_enabled != 0u && g_src < GAMMA_SOLID) {
+    float2 c = mul2(f2((float)x + 0.5f, (float)y + 0.5f), d.cell_w);
+    float2 v0 = fluid_velocity_at_world(d, c);
+    float h = rb_max(P->dt, 0.0f);
+    float2 c2 = f2(c.x + v0.x * d.wpf_x * h * 0.5f, c.y + v0.y * d.wpf_y * h * 0.5f);
+    v = fluid_velocity_at_world(d, c2);
+  }
+  if (v.x != 0.0f || v.y != 0.0f) {
+    bool rock_r = x + 1u < G && __ldg(d.gamma + idx + 1) >= GAMMA_SOLID;
+    bool rock_l = x > 0u && __ldg(d.gamma + idx - 1) >= GAMMA_SOLID;
+    bool rock_u = y + 1u < GH && __ldg(d.gamma + idx + G) >= GAMMA_SOLID;
+    bool rock_d = y > 0u && __ldg(d.gamma + idx - G) >= GAMMA_SOLID;
+    if ((v.x > 0.0f && rock_r) || (v.x < 0.0f && rock_l)) v.x = 0.0f;
+    else if ((v.x > 0.0f && rock_l) || (v.x < 0.0f && rock_r)) v.x *= 0.5f;
+    if ((v.y > 0.0f && rock_u) || (v.y < 0.0f && rock_d)) v.y = 0.0f;
+    else if ((v.y > 0.0f && rock_d) || (v.y < 0.0f && rock_u)) v.y *= 0.5f;
+  }
+  const float tn = (float)(P->transport_every > 1u ? P->transport_every : 1u);
+  const float dtp = rb_max(P->dt, 0.0f);
+  float2 disp = f2(v.x * d.sx * dtp * tn, v.y * d.sy * dtp * tn);
+  float agitation = rb_clamp(len2(v) / DIFF_AGITATION_SPEED, 0.0f, 1.0f);
+  float p_diff = rb_clamp(DIFF_HOP_P * rb_mix(DIFF_HOP_FLOOR, 1.0f, agitation) * rb_max(P->diffusion, 0.0f) * tn, 0.0f, 0.5f);
+  if (g_src > 0u) p_diff = rb_min(DIFF_HOP_P * BURIED_DIFF_FACTOR / (1.0f + GAMMA_POROSITY_K * (float)g_src) * tn, 0.5f);
+  const uint32_t cap_self = capacity_of(g_src);
+  if (src_total > cap_self) p_diff = rb_min(CHEM_SQUEEZE_P * tn, 0.5f);
+  float p_settle = 0.0f;
+  if (g_src == 0u) p_settle = rb_min(MONOMER_SETTLE_P * rb_max(P->settle, 0.0f) * tn, 0.5f);
+  const int base_x = rb_f2i(rb_floor(disp.x)) - 1, base_y = rb_f2i(rb_floor(disp.y)) - 1;
+
+  float press[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  float max_drop = 0.0f;
+  if (P->monomer_pressure > 0.0f) {
+    float f_self = (float)src_total / (float)(cap_self > 1u ? cap_self : 1u);
+    long nb[4] = {1, -1, (long)G, -(long)G};
+    bool inside[4] = {x + 1u < G, x > 0u, y + 1u < GH, y > 0u};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (!inside[k]) continue;
+      size_t n = (size_t)((long)idx + nb[k]);
+      uint32_t cap_n = capacity_of(__ldg(d.gamma + n));
+      if (cap_n == 0u) continue;
+      float f_n = (float)cell_total4(load_cell(d.chem, n)) / (float)cap_n;
+      press[k] = rb_max((float)0.05, 1.0f + P->monomer_pressure * (f_self - f_n));
+      max_drop = rb_max(max_drop, f_self - f_n);
+    }
+  }
+  p_diff = rb_clamp(p_diff + PRESSURE_HOP_P * P->monomer_pressure * max_drop * tn, 0.0f, 0.5f);
+  // uv_light_at_cell (light.wgsl:46-50)
+  const float light_t = d.light[(size_t)(umin(y, GH - 1u) / LIGHT_DIV) * d.lw + umin(x, G - 1u) / LIGHT_DIV];
+
+  float p_bound = 0.0f;
+  float accept[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  float accept_spent[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  if (P->aggregation > 0.0f && src_total <= cap_self) {
+    float e[5];
+    e[0] = (float)(d.agg_nb[idx] + d.agg_act[idx]);
+    e[1] = x + 1u < G ? (float)(d.agg_nb[idx + 1] + d.agg_act[idx + 1]) : 0.0f;
+    e[2] = x > 0u ? (float)(d.agg_nb[idx - 1] + d.agg_act[idx - 1]) : 0.0f;
+    e[3] = y + 1u < GH ? (float)(d.agg_nb[idx + G] + d.agg_act[idx + G]) : 0.0f;
+    e[4] = y > 0u ? (float)(d.agg_nb[idx - G] + d.agg_act[idx - G]) : 0.0f;
+    uint32_t fx = umin((x * (uint32_t)d.fw) / G, (uint32_t)d.fw - 1u);
+    uint32_t fy = umin((y * (uint32_t)d.fh) / GH, (uint32_t)d.fh - 1u);
+    float t_rel = 1.0f + rb_max(d.temp_in[(size_t)fy * d.fw + fx], 0.0f) / TEMP_ACT_THRESHOLD;
+    float room = rb_clamp(5.0f * (1.0f - (float)src_total / (float)(cap_self > 1u ? cap_self : 1u)), 0.0f, 1.0f);
+    float k_e = P->aggregation * room / t_rel;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      float drop = e[0] - e[k + 1];
+      if (drop > 0.0f) accept[k] = rb_exp(-k_e * drop);
+      float rise = e[k + 1] - e[0];
+      if (rise > 0.0f) accept_spent[k] = rb_exp(-k_e * rise);
+    }
+    p_bound = 1.0f - rb_exp(-k_e * rb_min(rb_max(e[0] - 1.0f, 0.0f), 48.0f));
+  }
+
+  const float2 bound_start = p_bound > 0.0f ? smooth_start(x, y, P) : f2(0.0f, 0.0f);
+  const bool disperse = g_src > 0u && (disp.x != 0.0f || disp.y != 0.0f);
+  const float disp_len = disperse ? len2(disp) : 0.0f;
+  uint32_t words[4] = {cw.x, cw.y, cw.z, cw.w};
+  for (uint32_t ch = 0; ch < 4; ch++) {
+    const uint32_t slot = (uint32_t)(idx * 4 + ch);
+    const uint32_t v_ch = words[ch];
+    uint32_t act_n = v_ch & CHEM_STATE_MASK;
+    uint32_t spent_n = v_ch >> 16;
+    if (act_n + spent_n == 0u) continue;
+    if (spent_n > 0u) {
+      float sens = 1.0f + CHEM_SENSITIZE * (float)umin(act_n, 8u);
+      float exp_act = (float)umin(spent_n, 8u) * tn *
+                      (LIGHT_ACT_P * rb_max(P->uv_strength, 0.0f) * rb_max(P->direct_photoactivation, 0.0f) * light_t * sens +
+                       rb_max(P->reactivation_rate, 0.0f));
+      uint32_t na = rb_f2u(rb_floor(exp_act));
+      float frac = exp_act - (float)na;
+      if (frac > 0.0f && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_PHOTO, P->seed).x) < frac) na += 1u;
+      na = umin(na, umin(spent_n, 8u));
+      act_n += na;
+      spent_n -= na;
+    }
+    if (act_n > 0u) {
+      float shield = 1.0f / (1.0f + CHEM_SHIELD * (float)(umin(act_n, 8u) - 1u));
+      float exp_dec = (float)umin(act_n, 8u) * rb_max(P->activation_decay, 0.0f) * shield * tn;
+      if (exp_dec > 0.0f && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_DECAY, P->seed).x) < exp_dec) {
+        act_n -= 1u;
+        spent_n += 1u;
+      }
+    }
+    float coh[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+    if (act_n > 0u && P->cohesion > 0.0f) {
+      if (x + 1u < G) coh[0] = 1.0f + P->cohesion * (float)umin(__ldg(d.chem + (idx + 1) * 4 + ch) & CHEM_STATE_MASK, 8u);
+      if (x > 0u) coh[1] = 1.0f + P->cohesion * (float)umin(__ldg(d.chem + (idx - 1) * 4 + ch) & CHEM_STATE_MASK, 8u);
+      if (y + 1u < GH) coh[2] = 1.0f + P->cohesion * (float)umin(__ldg(d.chem + (idx + G) * 4 + ch) & CHEM_STATE_MASK, 8u);
+      if (y > 0u) coh[3] = 1.0f + P->cohesion * (float)umin(__ldg(d.chem + (idx - G) * 4 + ch) & CHEM_STATE_MASK, 8u);
+    }
+    uint32_t bins[16];
+#pragma unroll
+    for (int b = 0; b < 16; b++) bins[b] = 0u;
+    uint32_t stay = 0;
+    const uint32_t n = act_n + spent_n;
+    const uint32_t movers = umin(n, MAX_MOVERS_PER_CH);
+    const uint32_t act_stay = act_n - umin(act_n, movers);
+    stay += act_stay + (n - movers - act_stay) * CHEM_SPENT_ONE;
+    for (uint32_t k = 0; k < movers; k++) {
+      const bool is_act = k < act_n;
+      const uint32_t unit = is_act ? 1u : CHEM_SPENT_ONE;
+      rb_u4 ru = rb_pcg4d(slot, P->epoch, RB_S_MOVE + k, P->seed);
+      float rfx = rb_u2f(ru.x), rfy = rb_u2f(ru.y), rfz = rb_u2f(ru.z), rfw = rb_u2f(ru.w);
+      bool bound = is_act && p_bound > 0.0f && rb_fract(rfz * (float)7.31 + rfw * (float)3.17) < p_bound;
+      float px = (bound ? bound_start.x : rfx) + disp.x;
+      float py = (bound ? bound_start.y : rfy) + disp.y;
+      if (disperse) {
+        rb_u4 rj = rb_pcg4d(slot, P->epoch, RB_S_DISPERSE + k, P->seed);
+        float jx = (rb_u2f(rj.x) * 2.0f - 1.0f) * disp_len * RUBBLE_DISPERSION;
+        float jy = (rb_u2f(rj.y) * 2.0f - 1.0f) * disp_len * RUBBLE_DISPERSION;
+        px += rb_clamp(jx, (float)-0.9, (float)0.9);
+        py += rb_clamp(jy, (float)-0.9, (float)0.9);
+      }
+      if (rfz < p_diff) {
+        float w0 = press[0], w1 = press[1], w2 = press[2], w3 = press[3];
+        if (is_act) {
+          w0 *= coh[0];
+          w1 *= coh[1];
+          w2 *= coh[2];
+          w3 *= coh[3];
+        }
+        float u = rfw * (w0 + w1 + w2 + w3);
+        uint32_t dd;
+        if (u < w0) dd = 0u;
+        else if ((u -= w0) < w1) dd = 1u;
+        else if ((u -= w1) < w2) dd = 2u;
+        else dd = 3u;
+        float acc_d = is_act ? accept[dd] : accept_spent[dd];
+        bool stay_put = rb_fract(rfw * (float)13.73 + rfx * (float)5.31) >= acc_d;
+        if (!stay_put) {
+          if (dd == 0u) px += 1.0f;
+          else if (dd == 1u) px -= 1.0f;
+          else if (dd == 2u) py += 1.0f;
+          else py -= 1.0f;
+        }
+      } else if (rfz < p_diff + p_settle) {
+        py -= 1.0f;
+      }
+      int offx = rb_f2i(rb_floor(px)) - base_x, offy = rb_f2i(rb_floor(py)) - base_y;
+      uint32_t bi = (uint32_t)iclamp(offy, 0, 3) * 4u + (uint32_t)iclamp(offx, 0, 3);
+      bins[bi] += unit;
+    }
+#pragma unroll
+    for (uint32_t b = 0; b < 16; b++) {
+      uint32_t cnt = bins[b];
+      if (cnt == 0u) continue;
+      int tx = iclamp((int)x + base_x + (int)(b & 3u), 0, (int)G - 1);
+      int ty = iclamp((int)y + base_y + (int)(b >> 2), 0, (int)GH - 1);
+      size_t t_idx = (size_t)ty * G + tx;
+      bool blocked = false;
+      if (t_idx != idx) {
+        uint32_t g_tgt = __ldg(d.gamma + t_idx);
+        if (g_tgt >= GAMMA_SOLID) blocked = g_src < GAMMA_SOLID;
+        else if (cell_total4(load_cell(d.chem, t_idx)) > capacity_of(g_tgt)) blocked = true;
+      }
+      if (blocked) stay += cnt;
+      else atomicAdd(d.chem_next + t_idx * 4 + ch, cnt);
+    }
+    if (stay > 0u) atomicAdd(d.chem_next + slot, stay);
+  }
+}
+
+// ledger.wgsl:225-245: per-block sums in registers and warp shuffles, then
+// one global atomic add per counter (u32, wrapping like the reference).
+__global__ void __launch_bounds__(256) k_ledger(const uint32_t* __restrict__ chem, size_t cells, uint32_t* out) {
+  uint32_t s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const uint4* c4 = reinterpret_cast<const uint4*>(chem);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += (size_t)gridDim.x * blockDim.x) {
+    uint4 c = __ldg(c4 + i);
+    s[0] += c.x & 0xFFFFu;
+    s[1] += c.y & 0xFFFFu;
+    s[2] += c.z & 0xFFFFu;
+    s[3] += c.w & 0xFFFFu;
+    s[4] += c.x >> 16;
+    s[5] += c.y >> 16;
+    s[6] += c.z >> 16;
+    s[7] += c.w >> 16;
+  }
+  __shared__ uint32_t red[8][8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    uint32_t v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    uint32_t v = 0;
+    for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++) v += red[wv][threadIdx.x];
+    if (v) atomicAdd(out + threadIdx.x, v);
+  }
+}
+
+}  // namespace
+
+inline double gc(const Dev& d) { return (double)d.gw * d.gh; }
+inline double fc(const Dev& d) { return (double)d.fw * d.fh; }
+
+void launch_slope(const Dev& d, float upc, cudaStream_t s) {
+  RB_LAUNCH("compute_gamma_slope", 12.0 * gc(d), s, k_slope<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, upc));
+}
+void launch_thermal(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
+  RB_LAUNCH("thermal_activation", 4.0 * fc(d), s, k_thermal<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, P));
+}
+void launch_agg(const Dev& d, cudaStream_t s) {
+  size_t cells = (size_t)d.gw * d.gh;
+  RB_LAUNCH("agg_count", 20.0 * gc(d), s, k_agg_count<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d));
+  RB_LAUNCH("agg_neighbours", 8.0 * gc(d), s, k_agg_neighbours<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d));
+}
+void launch_scatter(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
+  RB_LAUNCH("transport_scatter", 45.0 * gc(d) + 12.0 * fc(d), s, k_scatter<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, P));
+}
+void launch_ledger(const Dev& d, const uint32_t* chem, uint32_t* out12, cudaStream_t s) {
+  cudaMemsetAsync(out12, 0, 12 * sizeof(uint32_t), s);
+  size_t cells = (size_t)d.gw * d.gh;
+  unsigned blocks = (unsigned)((cells + 255) / 256);
+  if (blocks > 152u * 8u) blocks = 152u * 8u;
+  RB_LAUNCH("ledger_reduce", 16.0 * gc(d), s, k_ledger<<<blocks, 256, 0, s>>>(chem, cells, out12));
+}
+
+}  // namespace ribo

@@ -1,0 +1,332 @@
+"""Python mirror of the reference's world-step API over the C ABI.
+
+`World` follows the reference's `World` (src/world/mod.rs): it owns the
+device state, exposes `params` (SimParams) and `settings` (WorldSettings),
+`encode_steps(steps)` records steps and advances `params.epoch`, and
+`ledger_blocking()` / `read_cells_blocking()` / `read_f32_blocking(field)`
+read results back.  All compute runs in libribo_world.so (CUDA, sm_103a);
+loading fails loudly when the library is missing -- there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+HEADER = os.path.join(REPO, "include", "ribo_world.h")
+LIB_PATH = os.path.join(HERE, "_build", "libribo_world.so")
+
+# ribo_field
+CHEM, GAMMA, LIGHT, SLOPE, VELOCITY, PRESSURE, TEMP, REDOX, HEAT = range(9)
+VEL_SMOOTH, SOLID_MASK, DIVERGENCE, FORCE_VECTORS, REDOX_EATEN, NET_FLUX, SHADE = range(9, 16)
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "OVER_BUDGET", 4: "TIMEOUT", 5: "CUDA_ERROR"}
+MAX_STEPS_PER_FRAME = 64
+
+
+def _sim_param_fields():
+    """The SimParams field list, read from the C header (one source of truth)."""
+    text = open(HEADER).read()
+    body = re.search(r"typedef struct ribo_sim_params \{(.*?)\} ribo_sim_params;", text, re.S).group(1)
+    fields = []
+    for ty, name in re.findall(r"^\s*(uint32_t|float)\s+(\w+);", body, re.M):
+        fields.append((name, ctypes.c_uint32 if ty == "uint32_t" else ctypes.c_float))
+    return fields
+
+
+class SimParams(ctypes.Structure):
+    _fields_ = _sim_param_fields()
+
+    def copy(self) -> "SimParams":
+        c = SimParams()
+        ctypes.memmove(ctypes.byref(c), ctypes.byref(self), ctypes.sizeof(SimParams))
+        return c
+
+
+assert ctypes.sizeof(SimParams) == 464, ctypes.sizeof(SimParams)
+
+
+class WorldCfg(ctypes.Structure):
+    _fields_ = [
+        ("grid_w", ctypes.c_uint32), ("grid_h", ctypes.c_uint32),
+        ("fluid_w", ctypes.c_uint32), ("fluid_h", ctypes.c_uint32),
+        ("world_units_per_cell", ctypes.c_uint32), ("mg_min_size", ctypes.c_uint32),
+        ("mg_pre", ctypes.c_uint32), ("mg_post", ctypes.c_uint32), ("mg_coarse", ctypes.c_uint32),
+        ("precision_mode", ctypes.c_uint32), ("device", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 5),
+    ]
+
+
+class WorldSettings(ctypes.Structure):
+    _fields_ = [
+        ("fluid_enabled", ctypes.c_uint32), ("fluid_substep", ctypes.c_uint32),
+        ("multigrid", ctypes.c_uint32), ("mg_cycles", ctypes.c_uint32),
+        ("jacobi_iters", ctypes.c_uint32), ("ledger_each_step", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 2),
+    ]
+
+
+class KernelTiming(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_uint32), ("ms", ctypes.c_float),
+                ("bytes", ctypes.c_double)]
+
+
+class RiboError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libribo_world.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RiboError(f"{path} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+    lib = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    sig = {
+        "ribo_last_error": ([], ctypes.c_char_p),
+        "ribo_sim_params_default": ([P(SimParams)], None),
+        "ribo_world_settings_default": ([P(WorldSettings)], None),
+        "ribo_world_create": ([P(WorldCfg), P(vp)], ctypes.c_int),
+        "ribo_world_destroy": ([vp], None),
+        "ribo_world_set_settings": ([vp, P(WorldSettings)], ctypes.c_int),
+        "ribo_world_get_settings": ([vp, P(WorldSettings)], ctypes.c_int),
+        "ribo_world_upload": ([vp, ctypes.c_int, vp, ctypes.c_size_t], ctypes.c_int),
+        "ribo_world_read": ([vp, ctypes.c_int, vp, ctypes.c_size_t], ctypes.c_int),
+        "ribo_world_device_ptr": ([vp, ctypes.c_int, P(vp), P(ctypes.c_size_t)], ctypes.c_int),
+        "ribo_world_step": ([vp, P(SimParams), ctypes.c_uint32], ctypes.c_int),
+        "ribo_world_encode_steps": ([vp, P(SimParams), ctypes.c_uint32], ctypes.c_int),
+        "ribo_derive_step_params": ([P(SimParams), P(WorldSettings), ctypes.c_uint32, P(SimParams)], ctypes.c_int),
+        "ribo_world_ledger": ([vp, P(ctypes.c_uint32)], ctypes.c_int),
+        "ribo_world_sync": ([vp], ctypes.c_int),
+        "ribo_world_last_step_ms": ([vp, P(ctypes.c_float)], ctypes.c_int),
+        "ribo_world_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "ribo_world_read_kernel_timing": ([vp, P(KernelTiming), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
+        "ribo_kernel_launch_count": ([], ctypes.c_uint64),
+        "ribo_world_step_ledgers": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
+        "ribo_world_mark": ([vp, ctypes.c_uint32], ctypes.c_int),
+        "ribo_world_elapsed_ms": ([vp, ctypes.c_uint32, ctypes.c_uint32, P(ctypes.c_float)], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str = ""):
+    if status != 0:
+        msg = load_library().ribo_last_error().decode(errors="replace")
+        raise RiboError(f"{what}: {STATUS.get(status, status)}: {msg}")
+
+
+def kernel_launch_count() -> int:
+    return int(load_library().ribo_kernel_launch_count())
+
+
+def default_params(seed: int = 1) -> SimParams:
+    p = SimParams()
+    load_library().ribo_sim_params_default(ctypes.byref(p))
+    p.seed = seed
+    return p
+
+
+def default_settings() -> WorldSettings:
+    s = WorldSettings()
+    load_library().ribo_world_settings_default(ctypes.byref(s))
+    return s
+
+
+def derive_step_params(base: SimParams, settings: WorldSettings, steps: int):
+    out = (SimParams * steps)()
+    check(load_library().ribo_derive_step_params(ctypes.byref(base), ctypes.byref(settings), steps, out), "derive")
+    return out
+
+
+@dataclass
+class Ledger:
+    """Exact matter count per channel (A U G C) and state (src/world/mod.rs:39-82)."""
+
+    act: tuple
+    spent: tuple
+    held: tuple = (0, 0, 0, 0)
+
+    def total(self) -> int:
+        return sum(self.act) + sum(self.spent) + sum(self.held)
+
+    def channel(self, ch: int) -> int:
+        return self.act[ch] + self.spent[ch] + self.held[ch]
+
+    @staticmethod
+    def from_cells(cells: np.ndarray) -> "Ledger":
+        c = np.asarray(cells, dtype=np.uint32).reshape(-1, 4)
+        act = tuple(int(v) for v in (c & 0xFFFF).astype(np.uint64).sum(axis=0))
+        spent = tuple(int(v) for v in (c >> 16).astype(np.uint64).sum(axis=0))
+        return Ledger(act, spent)
+
+    @staticmethod
+    def from_words(w) -> "Ledger":
+        w = [int(v) for v in w]
+        return Ledger(tuple(w[0:4]), tuple(w[4:8]), tuple(w[8:12]))
+
+
+class World:
+    """One world on the GPU (the reference's `World`, hot-path part)."""
+
+    def __init__(self, grid, fluid=None, seed: int = 1, *, world_units_per_cell: int = 30,
+                 mg_min_size: int = 8, mg_pre: int = 2, mg_post: int = 2, mg_coarse: int = 30,
+                 precision_mode: int = 0, device: int = 0):
+        lib = load_library()
+        gw, gh = (grid, grid) if isinstance(grid, int) else grid
+        if fluid is None:
+            fluid = (gw, gh)
+        fw, fh = (fluid, fluid) if isinstance(fluid, int) else fluid
+        cfg = WorldCfg(gw, gh, fw, fh, world_units_per_cell, mg_min_size, mg_pre, mg_post, mg_coarse, precision_mode,
+                       device)
+        self.cfg = cfg
+        self.gw, self.gh, self.fw, self.fh = gw, gh, fw, fh
+        h = ctypes.c_void_p()
+        check(lib.ribo_world_create(ctypes.byref(cfg), ctypes.byref(h)), "ribo_world_create")
+        self._h = h
+        self._lib = lib
+        self.params = default_params(seed)
+        self.settings = default_settings()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ribo_world_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- sizes ----
+    @property
+    def cells(self) -> int:
+        return self.gw * self.gh
+
+    @property
+    def fluid_cells(self) -> int:
+        return self.fw * self.fh
+
+    def field_shape(self, field: int):
+        C, F, L = (self.gh, self.gw), (self.fh, self.fw), (self.gh // 2, self.gw // 2)
+        return {
+            CHEM: (C + (4,), np.uint32), GAMMA: (C, np.uint32), LIGHT: ((2,) + L, np.float32),
+            SLOPE: (C + (2,), np.float32), VELOCITY: (F + (2,), np.float32), PRESSURE: (F, np.float32),
+            TEMP: (F, np.float32), REDOX: (F, np.float32), HEAT: (F + (2,), np.float32),
+            VEL_SMOOTH: (F + (2,), np.float32), SOLID_MASK: (F, np.uint32), DIVERGENCE: (F, np.float32),
+            FORCE_VECTORS: (F + (2,), np.uint32), REDOX_EATEN: (F, np.uint32),
+            NET_FLUX: ((self.fh + self.fw,), np.float32), SHADE: ((2,) + L, np.uint32),
+        }[field]
+
+    # ---- data movement ----
+    def _sync_settings(self):
+        check(self._lib.ribo_world_set_settings(self._h, ctypes.byref(self.settings)), "settings")
+
+    def upload(self, field: int, array: np.ndarray):
+        shape, dt = self.field_shape(field)
+        a = np.ascontiguousarray(array, dtype=dt).reshape(shape)
+        check(self._lib.ribo_world_upload(self._h, field, a.ctypes.data, a.nbytes), f"upload {field}")
+
+    def read(self, field: int) -> np.ndarray:
+        shape, dt = self.field_shape(field)
+        a = np.empty(shape, dtype=dt)
+        check(self._lib.ribo_world_read(self._h, field, a.ctypes.data, a.nbytes), f"read {field}")
+        return a
+
+    def device_ptr(self, field: int):
+        p = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        check(self._lib.ribo_world_device_ptr(self._h, field, ctypes.byref(p), ctypes.byref(n)), "device_ptr")
+        return p.value, n.value
+
+    def read_cells_blocking(self) -> np.ndarray:
+        return self.read(CHEM).reshape(-1)
+
+    def read_f32_blocking(self, field: int) -> np.ndarray:
+        return self.read(field).reshape(-1).view(np.float32)
+
+    # ---- stepping ----
+    def step(self, per_step):
+        """Records len(per_step) steps with explicit per-step SimParams."""
+        self._sync_settings()
+        n = len(per_step)
+        arr = per_step if isinstance(per_step, ctypes.Array) else (SimParams * n)(*per_step)
+        check(self._lib.ribo_world_step(self._h, arr, n), "ribo_world_step")
+
+    def encode_steps(self, steps: int):
+        """World::encode_steps: derives per-step params and advances params.epoch."""
+        self._sync_settings()
+        check(self._lib.ribo_world_encode_steps(self._h, ctypes.byref(self.params), steps), "encode_steps")
+
+    def run(self, steps: int):
+        """Steps in batches of MAX_STEPS_PER_FRAME, like tests/conservation.rs::run."""
+        done = 0
+        while done < steps:
+            n = min(MAX_STEPS_PER_FRAME, steps - done)
+            self.encode_steps(n)
+            done += n
+
+    def sync(self):
+        check(self._lib.ribo_world_sync(self._h), "sync")
+
+    def last_step_ms(self) -> float:
+        ms = ctypes.c_float()
+        check(self._lib.ribo_world_last_step_ms(self._h, ctypes.byref(ms)), "last_step_ms")
+        return ms.value
+
+    def enable_kernel_timing(self, on: bool = True):
+        check(self._lib.ribo_world_enable_kernel_timing(self._h, 1 if on else 0), "kernel timing")
+
+    def read_kernel_timing(self):
+        """[(name, launches, ms, algorithmic bytes)] of the last step call."""
+        cap = 128
+        arr = (KernelTiming * cap)()
+        n = ctypes.c_uint32()
+        check(self._lib.ribo_world_read_kernel_timing(self._h, arr, cap, ctypes.byref(n)), "read timing")
+        return [(arr[i].name.decode(), arr[i].launches, arr[i].ms, arr[i].bytes) for i in range(min(n.value, cap))]
+
+    def step_ledgers(self, n: int):
+        """Ledgers after each of the last call's n steps (settings.ledger_each_step)."""
+        out = (ctypes.c_uint32 * (12 * n))()
+        check(self._lib.ribo_world_step_ledgers(self._h, out, n), "step ledgers")
+        return [Ledger.from_words(out[12 * i:12 * i + 12]) for i in range(n)]
+
+    def mark(self, slot: int):
+        check(self._lib.ribo_world_mark(self._h, slot), "mark")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = ctypes.c_float()
+        check(self._lib.ribo_world_elapsed_ms(self._h, a, b, ctypes.byref(ms)), "elapsed")
+        return ms.value
+
+    def ledger_blocking(self) -> Ledger:
+        out = (ctypes.c_uint32 * 12)()
+        check(self._lib.ribo_world_ledger(self._h, out), "ledger")
+        return Ledger.from_words(out)
+
+    def seed_inputs(self, inputs: dict):
+        """Uploads a dict {field: array} (e.g. from synth.make_world_inputs)."""
+        for f in (GAMMA, CHEM, LIGHT, VELOCITY, PRESSURE, TEMP, REDOX, HEAT, SHADE, FORCE_VECTORS, REDOX_EATEN):
+            if f in inputs:
+                self.upload(f, inputs[f])
