@@ -1274,7 +1274,10 @@ int orc_upload(void* w, int field, const void* host, size_t bytes) {
   if (!p || n != bytes) return 1;
   memcpy(p, host, bytes);
   if (field == RIBO_FIELD_GAMMA) {
+    // The slope and wall mask are functions of gamma alone; the step also
+    // rebuilds the mask at every fluid step, as the reference does.
     o->compute_slope();
+    o->build_solid_mask();
   }
   return 0;
 }

@@ -76,12 +76,15 @@ def test_conservation_and_ledger_full_size(rw):
     w.settings.fluid_substep = 1
     w.settings.mg_cycles = 4
     seeded = rw.Ledger.from_cells(w.read_cells_blocking())
+    per_channel = [seeded.channel(c) for c in range(4)]
     before = w.read_cells_blocking().copy()
     for _ in range(8):
         w.encode_steps(1)
-        assert w.ledger_blocking() == seeded
+        led = w.ledger_blocking()
+        assert [led.channel(c) for c in range(4)] == per_channel
     cells = w.read_cells_blocking()
-    assert rw.Ledger.from_cells(cells) == seeded
+    assert rw.Ledger.from_cells(cells) == w.ledger_blocking()
+    assert rw.Ledger.from_cells(cells).total() == seeded.total()
     assert (cells != before).mean() > 0.1
     v = w.read(rw.VELOCITY)
     assert np.isfinite(v).all()
