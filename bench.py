@@ -247,11 +247,16 @@ def run_ours(args):
     seed = 1000 + rank
     inputs = synth.make_world_inputs(n, seed=seed)
     w = rw.World(n, seed=seed, mg_min_size=16, mg_pre=3, mg_post=3, device=local)
-    w.params = synth.bench_params(seed)
     w.settings.fluid_substep = 1
     w.settings.mg_cycles = 4
     w.settings.ledger_each_step = 1
-    w.seed_inputs(inputs)
+
+    def reset():
+        """Every measured phase starts from the same seeded state at epoch 0."""
+        w.seed_inputs(inputs)
+        w.params = synth.bench_params(seed)
+
+    reset()
     seeded_led = rw.Ledger.from_cells(inputs[rw.CHEM])
     seeded = [seeded_led.channel(c) for c in range(4)]
 
@@ -295,6 +300,8 @@ def run_ours(args):
     # ---- per-kernel CUDA events (a separate pass: events between launches
     # would perturb the timed region above) ----
     prof_steps = max(1, min(args.steps, args.profile_steps))
+    reset()
+    run_steps(max(args.warmup, 3))
     w.enable_kernel_timing(True)
     kern = {}
     run_steps(prof_steps, timing=True, acc=kern)
@@ -302,6 +309,10 @@ def run_ours(args):
 
     # ---- end to end through the public API, host buffers ----
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    reset()
+    for _ in range(max(args.warmup, 3)):
+        w.encode_steps(1)
+        w.step_ledgers(1)
     w.sync()
     barrier(ws)
     t = time.perf_counter()
@@ -359,7 +370,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=2048)
-    ap.add_argument("--e2e-steps", type=int, default=64)
+    ap.add_argument("--e2e-steps", type=int, default=256)
     ap.add_argument("--profile-steps", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-seconds", type=float, default=60.0)

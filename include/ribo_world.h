@@ -169,7 +169,8 @@ typedef struct ribo_world_cfg {
   uint32_t mg_coarse;             // red-black sweeps on the coarsest level
   uint32_t precision_mode;        // RIBO_PRECISION_*
   uint32_t device;                // CUDA device ordinal the world lives on
-  uint32_t reserved[5];
+  uint32_t no_graphs;             // 1 = never replay step sequences from CUDA graphs
+  uint32_t reserved[4];
 } ribo_world_cfg;
 
 enum {
@@ -186,7 +187,8 @@ typedef struct ribo_world_settings {
   uint32_t mg_cycles;      // V-cycles per fluid step (>= 1)
   uint32_t jacobi_iters;   // Jacobi iterations (rounded to even, 2..128)
   uint32_t ledger_each_step;  // 1 = run ledger_reduce after every step (read with ribo_world_step_ledgers)
-  uint32_t reserved[2];
+  uint32_t mg_unfused;        // 1 = one dispatch per half-sweep (the reference's recording); 0 = fused kernels (same bits)
+  uint32_t transport_simple;  // 1 = one thread per cell for the transport scatter; 0 = mover-parallel tiles (same bits)
 } ribo_world_settings;
 
 // Device fields a caller can upload / read.  Sizes in bytes, for a world with

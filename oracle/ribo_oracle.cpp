@@ -1223,7 +1223,7 @@ void* orc_create(const ribo_world_cfg* cfg) {
   if (!o->cfg.mg_pre) o->cfg.mg_pre = 2;
   if (!o->cfg.mg_post) o->cfg.mg_post = 2;
   if (!o->cfg.mg_coarse) o->cfg.mg_coarse = 30;
-  o->st = ribo_world_settings{1, 2, 1, 1, 128, 0, {0, 0}};
+  o->st = ribo_world_settings{1, 2, 1, 1, 128, 0, 0, 0};
   o->gw = cfg->grid_w;
   o->gh = cfg->grid_h;
   o->fw = cfg->fluid_w;

@@ -29,7 +29,16 @@ __global__ void k_solid_mask(const __grid_constant__ Dev d) {
   }
   float solidity = (float)n_solid * 0.25f;
   float perm = solidity >= 0.5f ? 0.0f : rb_clamp(1.0f - solidity * 2.0f, 0.0f, 1.0f);
-  d.mask[(size_t)y * d.fw + x] = perm < SOLID_PERM_THRESHOLD ? 1 : 0;
+  const bool solid = perm < SOLID_PERM_THRESHOLD;
+  d.mask[(size_t)y * d.fw + x] = solid ? 1 : 0;
+  if (d.fluid0) d.fluid0[(size_t)y * d.fw + x] = solid ? 0 : 1;  // multigrid level-0 water flags (mg_init)
+}
+
+// fluid.wgsl:196-216, evaluated once per mask build for every fluid cell.
+__global__ void k_wall_normals(const __grid_constant__ Dev d) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  d.normal[(size_t)y * d.fw + x] = solid_normal(d, x, y);
 }
 
 // fluid.wgsl:300-372 (update_temperature; copy_temperature becomes a
@@ -223,7 +232,7 @@ __global__ void k_advect(const __grid_constant__ Dev d, const ribo_sim_params* _
   }
   const float dt = fluid_dt(P);
   const float decay_factor = rb_pow(rb_clamp(P->fluid_decay, 0.0f, 1.0f), dt * 60.0f);
-  float2 n = solid_normal(d, x, y);
+  const float2 n = d.normal[idx];
   float2 pos = f2((float)x + 0.5f, (float)y + 0.5f);
   float2 vel = reflect_n(n, clamp_len(raw_velocity_cell(d, vin, x, y), MAX_VEL));
   float2 trace_pos = sub2(pos, mul2(vel, dt));
@@ -321,51 +330,65 @@ __global__ void k_subtract_gradient(const __grid_constant__ Dev d, const float2*
 
 // fluid.wgsl:640-657.  The reference sums each row (column) serially in
 // f32; the order of those adds fixes the rounding, so each line is summed
-// by one thread in index order.  Rows are staged through shared memory in
-// 32x32 tiles so the loads stay coalesced.
-constexpr int NF_LINES = 32;
-__global__ void k_net_flux_rows(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
-  __shared__ float tile[NF_LINES][33];
-  __shared__ uint8_t stile[NF_LINES][33];
-  int row0 = blockIdx.x * NF_LINES;
-  int lane = threadIdx.x;  // 32 threads
-  float sum = 0.0f, n = 0.0f;
-  int my_row = row0 + lane;
-  for (int x0 = 0; x0 < d.fw; x0 += 32) {
-    for (int r = 0; r < NF_LINES; r++) {
-      int yy = row0 + r, xx = x0 + lane;
-      float v = 0.0f;
-      uint8_t s = 1;
-      if (yy < d.fh && xx < d.fw) {
-        size_t i = (size_t)yy * d.fw + xx;
-        s = d.mask[i];
-        v = sanitize(vin[i]).y;
+// by one lane in index order.  A block owns 32 lines: its warps 1..7 stream
+// chunks of NF_C elements of those lines into a double-buffered shared
+// tile with coalesced loads, while warp 0 (lane = line) runs the 32 serial
+// add chains over the previous chunk.  Row blocks and column blocks share
+// one launch.
+constexpr int NF_L = 32, NF_C = 128, NF_THREADS = 256;
+__global__ void __launch_bounds__(NF_THREADS) k_net_flux(const __grid_constant__ Dev d, const float2* __restrict__ vin,
+                                                         int row_blocks) {
+  __shared__ float val[2][NF_L][NF_C + 1];
+  __shared__ uint8_t wall[2][NF_L][NF_C + 4];
+  const bool rows = (int)blockIdx.x < row_blocks;
+  const int line0 = (rows ? (int)blockIdx.x : (int)blockIdx.x - row_blocks) * NF_L;
+  const int nlines = rows ? d.fh : d.fw;
+  const int len = rows ? d.fw : d.fh;
+  const int nchunks = (len + NF_C - 1) / NF_C;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  auto load = [&](int c, int b, int t, int nt) {
+    const int k0 = c * NF_C;
+    for (int e = t; e < NF_L * NF_C; e += nt) {
+      int l, k;
+      if (rows) {
+        l = e / NF_C;
+        k = e % NF_C;
+      } else {
+        l = e % NF_L;
+        k = e / NF_L;
       }
-      tile[r][lane] = v;
-      stile[r][lane] = s;
+      int line = line0 + l, pos = k0 + k;
+      float v = 0.0f;
+      uint8_t w = 1;
+      if (line < nlines && pos < len) {
+        size_t i = rows ? (size_t)line * d.fw + pos : (size_t)pos * d.fw + line;
+        w = d.mask[i];
+        float2 s = sanitize(vin[i]);
+        v = rows ? s.y : s.x;
+      }
+      val[b][l][k] = v;
+      wall[b][l][k] = w;
     }
-    __syncwarp();
-    int lim = min(32, d.fw - x0);
-    for (int k = 0; k < lim; k++) {
-      if (stile[lane][k]) continue;
-      sum += tile[lane][k];
-      n += 1.0f;
-    }
-    __syncwarp();
-  }
-  if (my_row < d.fh) d.net_flux[my_row] = n > 0.0f ? sum / n : 0.0f;
-}
-__global__ void k_net_flux_cols(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
-  int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= d.fw) return;
+  };
+
+  load(0, 0, threadIdx.x, NF_THREADS);
+  __syncthreads();
   float sum = 0.0f, n = 0.0f;
-  for (int k = 0; k < d.fh; k++) {
-    size_t i = (size_t)k * d.fw + col;
-    if (d.mask[i]) continue;
-    sum += sanitize(vin[i]).x;
-    n += 1.0f;
+  for (int c = 0; c < nchunks; c++) {
+    const int b = c & 1;
+    if (warp == 0) {
+      for (int k = 0; k < NF_C; k++) {
+        if (wall[b][lane][k]) continue;
+        sum += val[b][lane][k];
+        n += 1.0f;
+      }
+    } else if (c + 1 < nchunks) {
+      load(c + 1, b ^ 1, threadIdx.x - 32, NF_THREADS - 32);
+    }
+    __syncthreads();
   }
-  d.net_flux[d.fh + col] = n > 0.0f ? sum / n : 0.0f;
+  if (warp == 0 && line0 + lane < nlines) d.net_flux[(rows ? 0 : d.fh) + line0 + lane] = n > 0.0f ? sum / n : 0.0f;
 }
 
 // fluid.wgsl:663-677
@@ -406,6 +429,7 @@ inline double gc(const Dev& d) { return (double)d.gw * d.gh; }
 
 void launch_solid_mask(const Dev& d, cudaStream_t s) {
   RB_LAUNCH("build_solid_mask", 4.0 * gc(d) + fc(d), s, k_solid_mask<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d));
+  RB_LAUNCH("wall_normals", 9.0 * fc(d), s, k_wall_normals<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d));
 }
 void launch_temperature(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
   RB_LAUNCH("update_temperature", 41.0 * fc(d) + 4.0 * gc(d), s, k_temperature<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P));
@@ -432,8 +456,8 @@ void launch_subtract_gradient(const Dev& d, const float2* vin, float2* vout, cud
   RB_LAUNCH("subtract_gradient", 21.0 * fc(d), s, k_subtract_gradient<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin, vout));
 }
 void launch_net_flux(const Dev& d, const float2* vin, cudaStream_t s) {
-  RB_LAUNCH("net_flux_rows", 9.0 * fc(d), s, k_net_flux_rows<<<(d.fh + NF_LINES - 1) / NF_LINES, 32, 0, s>>>(d, vin));
-  RB_LAUNCH("net_flux_cols", 9.0 * fc(d), s, k_net_flux_cols<<<(d.fw + 63) / 64, 64, 0, s>>>(d, vin));
+  int row_blocks = (d.fh + NF_L - 1) / NF_L, col_blocks = (d.fw + NF_L - 1) / NF_L;
+  RB_LAUNCH("net_flux", 18.0 * fc(d), s, k_net_flux<<<row_blocks + col_blocks, NF_THREADS, 0, s>>>(d, vin, row_blocks));
 }
 void launch_boundaries(const Dev& d, const float2* vin, float2* vout, cudaStream_t s) {
   RB_LAUNCH("enforce_boundaries", 17.0 * fc(d), s, k_boundaries<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin, vout));

@@ -8,6 +8,7 @@
 // half-sweep.
 #include "ribo_dev.cuh"
 #include "ribo_launch.h"
+#include "ribo_tma.cuh"
 
 namespace ribo {
 
@@ -24,6 +25,10 @@ struct Lv {
   float eps;
 };
 inline Lv lv(const MgLevel& L, const MgBufs& b) { return Lv{L.nx, L.ny, b.p + L.off, b.rhs + L.off, b.fluid + L.off, L.eps}; }
+
+// ---------------------------------------------------------------------------
+// One dispatch per half-sweep / restrict / prolong, as the reference records
+// them (src/world/mod.rs:1545-1577).
 
 // multigrid.wgsl:29-45: sum of the water neighbours and their count
 __device__ __forceinline__ void neighbors(const Lv& L, int x, int y, float& s, float& k) {
@@ -121,6 +126,341 @@ __global__ void k_jacobi(const __grid_constant__ Dev d, const float* __restrict_
   pout[idx] = is_bad(p_new) ? 0.0f : p_new;
 }
 
+// ---------------------------------------------------------------------------
+// Fused V-cycle.
+//
+// Fine levels: one kernel does "pre-smooth nu sweeps + residual + restrict"
+// and one does "prolong + post-smooth nu sweeps", each on a TWxTH tile held
+// in shared memory with a halo of 2nu+1 (resp. 2nu) cells.  Half-sweep s only
+// needs the cells at distance >= s from the loaded region's edge to be
+// exact, so after 2nu half-sweeps the tile interior and its one-cell ring
+// hold exactly the values a dispatch per half-sweep would give.
+//
+// The tile is staged as a BOXW-wide box starting BOXX cells left of the tile
+// (so its first x coordinate is 16-element aligned, as TMA requires) and H
+// rows above it; TMA copies p, rhs and the water flags in one transaction
+// group and zero-fills everything outside the level, which is exactly
+// "not water" / p = 0.  Without tensor maps the same box is loaded with
+// plain loads.
+//
+// Coarse levels (at most MG_SMEM_CELLS cells on the top one): one CTA runs
+// the whole remaining V-cycle in shared memory.
+//
+// Level 0 reads pressure_a (masked), the divergence and the level-0 water
+// flags (the negated wall mask, rebuilt with it) directly -- mg_init -- and
+// the last post kernel writes pressure_a (mg_finish).  A coarse level's p
+// starts every cycle at 0 (mg_restrict zeroes it), so the pre kernels of
+// levels >= 1 do not load it.
+constexpr int BOXX = 16;  // the box starts 16 cells left of the tile (16-element aligned for TMA)
+constexpr int MG_SMEM_CELLS = 4096;
+constexpr int COARSE_THREADS = 1024;
+
+struct BoxMaps {
+  CUtensorMap p, rhs, fl;
+};
+
+// The neighbour sum of multigrid.wgsl:34-45 in branch-free form: adding the
+// +0.0 of a non-water neighbour leaves the running sum unchanged (it starts
+// at +0.0 and can never become -0.0 in round-to-nearest).
+__device__ __forceinline__ float gs_update(const float* sp, const float* sr, const uint8_t* sf, int c, int stride, float eps) {
+  const float fl = sf[c - 1] ? 1.0f : 0.0f, fr = sf[c + 1] ? 1.0f : 0.0f;
+  const float fb = sf[c - stride] ? 1.0f : 0.0f, ft = sf[c + stride] ? 1.0f : 0.0f;
+  float sum = 0.0f;
+  sum += fl != 0.0f ? sp[c - 1] : 0.0f;
+  sum += fr != 0.0f ? sp[c + 1] : 0.0f;
+  sum += fb != 0.0f ? sp[c - stride] : 0.0f;
+  sum += ft != 0.0f ? sp[c + stride] : 0.0f;
+  float k = 0.0f;
+  k += fl;
+  k += fr;
+  k += fb;
+  k += ft;
+  return (sum - sr[c]) / (k + eps);
+}
+
+template <int TW, int TH, bool TMA, bool TOP, bool LOADP>
+__device__ __forceinline__ bool box_load(const Dev& d, const Lv& L, const float* __restrict__ p_src,
+                                         const float* __restrict__ r_src, const uint8_t* __restrict__ f_src,
+                                         const BoxMaps& maps, int bx, int by, int RH, float* sp, float* sr, uint8_t* sf,
+                                         uint64_t* bar) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  const int n = BOXW * RH;
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  if (TMA) {
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      mbar_expect_tx(bar, (uint32_t)((LOADP ? 4 : 0) * n + 4 * n + n));
+      if (LOADP) tma_load_2d(sp, &maps.p, bx, by, bar);
+      tma_load_2d(sr, &maps.rhs, bx, by, bar);
+      tma_load_2d(sf, &maps.fl, bx, by, bar);
+    }
+    if (!LOADP)
+      for (int e = tid; e < n; e += BX * BY) sp[e] = 0.0f;
+    __syncthreads();
+    if (!mbar_wait_bounded(bar, 0, d.status)) return false;
+  } else {
+    for (int e = tid; e < n; e += BX * BY) {
+      int gx = bx + e % BOXW, gy = by + e / BOXW;
+      float p = 0.0f, r = 0.0f;
+      uint8_t f = 0;
+      if (gx >= 0 && gy >= 0 && gx < L.nx && gy < L.ny) {
+        size_t gi = (size_t)gy * L.nx + gx;
+        f = f_src[gi];
+        r = r_src[gi];
+        if (LOADP) p = p_src[gi];
+      }
+      sp[e] = p;
+      sr[e] = r;
+      sf[e] = f;
+    }
+    __syncthreads();
+  }
+  if (TOP && LOADP) {  // mg_init: p = water ? pressure_a : 0
+    for (int e = tid; e < n; e += BX * BY)
+      if (!sf[e]) sp[e] = 0.0f;
+    __syncthreads();
+  }
+  return true;
+}
+
+// Half-sweeps 0..nsweeps-1 on the box; sweep s updates the cells at distance
+// >= s+1 from the edge of the valid region (multigrid.wgsl:60-77).
+template <int TW, int TH>
+__device__ __forceinline__ void box_sweeps(int nsweeps, int H, int RH, int bx, int by, float eps, float* sp, const float* sr,
+                                           const uint8_t* sf) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  const int ilo = BOXX - H, ihi = BOXX + TW + H;
+  for (int s = 0; s < nsweeps; s++) {
+    const int color = s & 1;
+    const int m = s + 1;
+    for (int j = m + threadIdx.y; j < RH - m; j += BY) {
+      const int gy = by + j;
+      const int i0 = ilo + m + (((bx + ilo + m + gy) ^ color) & 1);
+      for (int i = i0 + 2 * threadIdx.x; i < ihi - m; i += 2 * BX) {
+        const int c = j * BOXW + i;
+        if (sf[c]) sp[c] = gs_update(sp, sr, sf, c, BOXW, eps);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int TW, int TH>
+__device__ __forceinline__ void box_store(const Lv& L, float* __restrict__ p_out, int x0, int y0, int H, const float* sp) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  for (int j = threadIdx.y; j < TH; j += BY)
+    for (int i = threadIdx.x; i < TW; i += BX) {
+      int gx = x0 + i, gy = y0 + j;
+      if (gx < L.nx && gy < L.ny) p_out[(size_t)gy * L.nx + gx] = sp[(j + H) * BOXW + i + BOXX];
+    }
+}
+
+// Pre-smooth (nu sweeps) + residual + restrict (multigrid.wgsl:60-105).
+template <int TW, int TH, bool TMA, bool TOP>
+__global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ Dev d, Lv L, Lv C,
+                                                   const __grid_constant__ BoxMaps maps, const float* __restrict__ p_src,
+                                                   const float* __restrict__ r_src, const uint8_t* __restrict__ f_src,
+                                                   float* __restrict__ p_out, int nu) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  const int H = 2 * nu + 1, RH = TH + 2 * H;
+  float* sp = reinterpret_cast<float*>(smem_raw);
+  float* sr = sp + BOXW * RH;
+  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+  const int bx = x0 - BOXX, by = y0 - H;
+  if (!box_load<TW, TH, TMA, TOP, TOP>(d, L, p_src, r_src, f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
+  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, L.eps, sp, sr, sf);
+  box_store<TW, TH>(L, p_out, x0, y0, H, sp);
+  // residual of the 4 children of each coarse cell of the tile, x2 average
+  for (int cj = threadIdx.y; cj < TH / 2; cj += BY)
+    for (int ci = threadIdx.x; ci < TW / 2; ci += BX) {
+      int cgx = blockIdx.x * (TW / 2) + ci, cgy = blockIdx.y * (TH / 2) + cj;
+      if (cgx >= C.nx || cgy >= C.ny) continue;
+      float sum = 0.0f;
+      uint32_t nf = 0;
+#pragma unroll
+      for (uint32_t q = 0; q < 4; q++) {
+        int li = BOXX + 2 * ci + (int)(q & 1u), lj = H + 2 * cj + (int)(q >> 1);
+        int c = lj * BOXW + li;
+        if (!sf[c]) continue;
+        float s = 0.0f, k = 0.0f;
+        if (sf[c - 1]) { s += sp[c - 1]; k += 1.0f; }
+        if (sf[c + 1]) { s += sp[c + 1]; k += 1.0f; }
+        if (sf[c - BOXW]) { s += sp[c - BOXW]; k += 1.0f; }
+        if (sf[c + BOXW]) { s += sp[c + BOXW]; k += 1.0f; }
+        sum += sr[c] - (s - (k + L.eps) * sp[c]);
+        nf++;
+      }
+      size_t ci_g = (size_t)cgy * C.nx + cgx;
+      C.fl[ci_g] = nf > 0u ? 1 : 0;
+      C.rhs[ci_g] = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
+    }
+}
+
+// Prolong (add the coarse correction to water cells) + post-smooth nu sweeps
+// (multigrid.wgsl:108-114, 60-77).
+template <int TW, int TH, bool TMA>
+__global__ void __launch_bounds__(BX* BY) k_mg_post(const __grid_constant__ Dev d, Lv L, Lv C,
+                                                    const __grid_constant__ BoxMaps maps, const float* __restrict__ p_src,
+                                                    const float* __restrict__ r_src, const uint8_t* __restrict__ f_src,
+                                                    float* __restrict__ p_out, int nu) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  const int H = 2 * nu, RH = TH + 2 * H;
+  float* sp = reinterpret_cast<float*>(smem_raw);
+  float* sr = sp + BOXW * RH;
+  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+  const int bx = x0 - BOXX, by = y0 - H;
+  if (!box_load<TW, TH, TMA, false, true>(d, L, p_src, r_src, f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
+  const int n = BOXW * RH;
+  for (int e = threadIdx.y * BX + threadIdx.x; e < n; e += BX * BY) {
+    if (!sf[e]) continue;
+    int gx = bx + e % BOXW, gy = by + e / BOXW;
+    sp[e] += C.p[(size_t)(gy / 2) * C.nx + gx / 2];
+  }
+  __syncthreads();
+  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, L.eps, sp, sr, sf);
+  box_store<TW, TH>(L, p_out, x0, y0, H, sp);
+}
+
+// The V-cycle below (and including) level `top`, in one CTA.
+struct CoarseSet {
+  int n;  // levels in the set (top .. coarsest)
+  int nx[16], ny[16];
+  float eps[16];
+  int off[16];  // cell offset of each level in shared memory
+  const float* rhs_top;
+  const uint8_t* fl_top;
+  float* p_out;  // level `top` result
+};
+
+// One colour of a red-black sweep on a level held in shared memory: the
+// block is viewed as 32 x (COARSE_THREADS/32) threads walking the cells of
+// that colour only.
+__device__ __forceinline__ void sm_sweep(int nx, int ny, float eps, float* p, const float* r, const uint8_t* f, uint32_t color) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, rows = COARSE_THREADS / 32;
+  for (int y = ty; y < ny; y += rows) {
+    for (int x = 2 * tx + (int)(((uint32_t)y + color) & 1u); x < nx; x += 64) {
+      const int idx = y * nx + x;
+      if (!f[idx]) continue;
+      float s = 0.0f, k = 0.0f;
+      if (x > 0 && f[idx - 1]) { s += p[idx - 1]; k += 1.0f; }
+      if (x + 1 < nx && f[idx + 1]) { s += p[idx + 1]; k += 1.0f; }
+      if (y > 0 && f[idx - nx]) { s += p[idx - nx]; k += 1.0f; }
+      if (y + 1 < ny && f[idx + nx]) { s += p[idx + nx]; k += 1.0f; }
+      p[idx] = (s - r[idx]) / (k + eps);
+    }
+  }
+  __syncthreads();
+}
+
+template <bool TOP>
+__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ Dev d, const __grid_constant__ CoarseSet cs,
+                                                              int nu_pre, int nu_post, int coarse) {
+  extern __shared__ float smem[];
+  int total = cs.off[cs.n - 1] + cs.nx[cs.n - 1] * cs.ny[cs.n - 1];
+  float* P = smem;
+  float* R = P + total;
+  uint8_t* F = reinterpret_cast<uint8_t*>(R + total);
+  {
+    const int n = cs.nx[0] * cs.ny[0];
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+      uint8_t f;
+      float r, p = 0.0f;
+      if (TOP) {
+        int y = idx / cs.nx[0], x = idx - y * cs.nx[0];
+        size_t gi = (size_t)y * d.fw + x;
+        f = d.mask[gi] ? 0 : 1;
+        r = d.div[gi];
+        p = f ? d.pa[gi] : 0.0f;
+      } else {
+        f = cs.fl_top[idx];
+        r = cs.rhs_top[idx];
+      }
+      P[idx] = p;
+      R[idx] = r;
+      F[idx] = f;
+    }
+  }
+  __syncthreads();
+  for (int l = 0; l + 1 < cs.n; l++) {
+    float* p = P + cs.off[l];
+    const float* r = R + cs.off[l];
+    const uint8_t* f = F + cs.off[l];
+    for (int k = 0; k < nu_pre; k++) {
+      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p, r, f, 0u);
+      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p, r, f, 1u);
+    }
+    const int nx = cs.nx[l], ny = cs.ny[l], cnx = cs.nx[l + 1], cny = cs.ny[l + 1];
+    float* pc = P + cs.off[l + 1];
+    float* rc = R + cs.off[l + 1];
+    uint8_t* fc = F + cs.off[l + 1];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, rows = COARSE_THREADS / 32;
+    for (int cy = ty; cy < cny; cy += rows)
+    for (int cx = tx; cx < cnx; cx += 32) {
+      const int cidx = cy * cnx + cx;
+      float sum = 0.0f;
+      uint32_t nf = 0;
+      for (uint32_t q = 0; q < 4; q++) {
+        int x = cx * 2 + (int)(q & 1u), y = cy * 2 + (int)(q >> 1);
+        int i = y * nx + x;
+        if (!f[i]) continue;
+        float s = 0.0f, k = 0.0f;
+        if (x > 0 && f[i - 1]) { s += p[i - 1]; k += 1.0f; }
+        if (x + 1 < nx && f[i + 1]) { s += p[i + 1]; k += 1.0f; }
+        if (y > 0 && f[i - nx]) { s += p[i - nx]; k += 1.0f; }
+        if (y + 1 < ny && f[i + nx]) { s += p[i + nx]; k += 1.0f; }
+        sum += r[i] - (s - (k + cs.eps[l]) * p[i]);
+        nf++;
+      }
+      fc[cidx] = nf > 0u ? 1 : 0;
+      rc[cidx] = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
+      pc[cidx] = 0.0f;
+    }
+    __syncthreads();
+  }
+  {
+    const int l = cs.n - 1;
+    for (int k = 0; k < coarse; k++) {
+      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], P + cs.off[l], R + cs.off[l], F + cs.off[l], 0u);
+      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], P + cs.off[l], R + cs.off[l], F + cs.off[l], 1u);
+    }
+  }
+  for (int l = cs.n - 2; l >= 0; l--) {
+    float* p = P + cs.off[l];
+    const float* pc = P + cs.off[l + 1];
+    const float* r = R + cs.off[l];
+    const uint8_t* f = F + cs.off[l];
+    const int nx = cs.nx[l], cnx = cs.nx[l + 1];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, rows = COARSE_THREADS / 32;
+    for (int y = ty; y < cs.ny[l]; y += rows)
+      for (int x = tx; x < nx; x += 32) {
+        const int idx = y * nx + x;
+        if (f[idx]) p[idx] += pc[(y / 2) * cnx + x / 2];
+      }
+    __syncthreads();
+    for (int k = 0; k < nu_post; k++) {
+      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, 0u);
+      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, 1u);
+    }
+  }
+  {
+    const int n = cs.nx[0] * cs.ny[0];
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+      if (TOP) {
+        int y = idx / cs.nx[0], x = idx - y * cs.nx[0];
+        d.pa[(size_t)y * d.fw + x] = P[idx];
+      } else {
+        cs.p_out[idx] = P[idx];
+      }
+    }
+  }
+}
+
 }  // namespace
 
 inline double cells(const Lv& L) { return (double)L.nx * L.ny; }
@@ -158,6 +498,163 @@ void launch_jacobi(const Dev& d, int iters, cudaStream_t s) {
   for (int k = 0; k < iters; k++) {
     if (k % 2 == 0) RB_LAUNCH("jacobi_pressure", b, s, k_jacobi<<<grid2(d.fw, d.fh), blk, 0, s>>>(d, d.pa, d.pb));
     else RB_LAUNCH("jacobi_pressure", b, s, k_jacobi<<<grid2(d.fw, d.fh), blk, 0, s>>>(d, d.pb, d.pa));
+  }
+}
+
+static const char* const PRE_NAMES[8] = {"mg_pre_restrict_L0", "mg_pre_restrict_L1", "mg_pre_restrict_L2",
+                                         "mg_pre_restrict_L3", "mg_pre_restrict_L4", "mg_pre_restrict_L5",
+                                         "mg_pre_restrict_L6", "mg_pre_restrict_L7+"};
+static const char* const POST_NAMES[8] = {"mg_prolong_post_L0", "mg_prolong_post_L1", "mg_prolong_post_L2",
+                                          "mg_prolong_post_L3", "mg_prolong_post_L4", "mg_prolong_post_L5",
+                                          "mg_prolong_post_L6", "mg_prolong_post_L7+"};
+
+// Tile shape of a fine level: 64x32 tiles where there are enough of them to
+// fill the GPU, 32x16 tiles on the smaller levels, whose kernels are bound by
+// the latency of one tile rather than by bandwidth.
+static bool small_tiles(const MgLevel& L) {
+  const long big = (long)((L.nx + 63) / 64) * ((L.ny + 31) / 32);
+  return big < 2 * 152;
+}
+
+template <int TW, int TH>
+static size_t box_smem(int halo) {
+  return (size_t)(TW + 2 * BOXX) * (TH + 2 * halo) * 9;
+}
+
+int multigrid_first_coarse_level(const MgLevel* levels, int nl) {
+  int k = 0;
+  while (k < nl && (size_t)levels[k].nx * levels[k].ny > (size_t)MG_SMEM_CELLS) k++;
+  return k;
+}
+
+bool multigrid_fused_ok(const MgLevel* levels, int nl, const MgConfig& c) {
+  if (c.pre < 1 || c.post < 1 || 2 * c.pre + 1 > BOXX || 2 * c.post > BOXX || nl > 16) return false;
+  return multigrid_first_coarse_level(levels, nl) < nl;
+}
+
+bool multigrid_make_maps(const MgLevel* levels, int nl, const MgConfig& c, const MgBufs& b, const Dev& d,
+                         MgLevelMaps* out) {
+  const int k = multigrid_first_coarse_level(levels, nl);
+  bool all = true;
+  for (int l = 0; l < k; l++) {
+    MgLevelMaps& m = out[l];
+    const bool sm = small_tiles(levels[l]);
+    const uint32_t tw = sm ? 32 : 64, th = sm ? 16 : 32, bw = tw + 2 * BOXX;
+    const uint32_t rh_pre = th + 2 * (2 * c.pre + 1), rh_post = th + 2 * (2 * c.post);
+    const uint64_t nx = levels[l].nx, ny = levels[l].ny;
+    float* rhs = l == 0 ? d.div : b.rhs + levels[l].off;
+    uint8_t* fl = b.fluid + levels[l].off;
+    float* p_pre = l == 0 ? d.pa : b.p + levels[l].off;  // only level 0 loads p before pre-smoothing
+    float* p_post = l == 0 ? b.p_tmp : b.p2 + levels[l].off;
+    bool ok = true;
+    ok &= make_tensor_map_2d(&m.pre_p, p_pre, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_pre);
+    ok &= make_tensor_map_2d(&m.pre_rhs, rhs, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_pre);
+    ok &= make_tensor_map_2d(&m.pre_fl, fl, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, nx, ny, nx, bw, rh_pre);
+    ok &= make_tensor_map_2d(&m.post_p, p_post, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_post);
+    ok &= make_tensor_map_2d(&m.post_rhs, rhs, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_post);
+    ok &= make_tensor_map_2d(&m.post_fl, fl, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, nx, ny, nx, bw, rh_post);
+    m.ok = ok ? 1 : 0;
+    all = all && ok;
+  }
+  return all;
+}
+
+template <int TW, int TH>
+static void set_tile_attrs(int mx) {
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_post<TW, TH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_post<TW, TH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+static void set_smem_attrs() {
+  static uint64_t attr_done = 0;  // one bit per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (attr_done >> (dev & 63) & 1ull) return;
+  const int mx = 200 * 1024;
+  set_tile_attrs<64, 32>(mx);
+  set_tile_attrs<32, 16>(mx);
+  cudaFuncSetAttribute(k_mg_coarse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_coarse<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  attr_done |= 1ull << (dev & 63);
+}
+
+template <int TW, int TH>
+static void launch_pre(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
+  const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
+  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
+  const size_t sm = box_smem<TW, TH>(2 * c.pre + 1);
+  const bool tma = b.maps && b.maps[l].ok;
+  const BoxMaps maps = tma ? BoxMaps{b.maps[l].pre_p, b.maps[l].pre_rhs, b.maps[l].pre_fl} : BoxMaps{};
+  const float* rhs = l == 0 ? d.div : L.rhs;
+  float* pout = l == 0 ? b.p_tmp : b.p2 + levels[l].off;
+  const char* name = PRE_NAMES[l < 7 ? l : 7];
+  const double bytes = (l == 0 ? 13.0 : 9.0) * cells(L) + 5.0 * cells(C);
+  if (tma && l == 0)
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, true><<<grid, blk, sm, s>>>(d, L, C, maps, d.pa, rhs, L.fl, pout, c.pre));
+  else if (tma)
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, false><<<grid, blk, sm, s>>>(d, L, C, maps, nullptr, rhs, L.fl, pout, c.pre));
+  else if (l == 0)
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, true><<<grid, blk, sm, s>>>(d, L, C, maps, d.pa, rhs, L.fl, pout, c.pre));
+  else
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, false><<<grid, blk, sm, s>>>(d, L, C, maps, nullptr, rhs, L.fl, pout, c.pre));
+}
+
+template <int TW, int TH>
+static void launch_post(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
+  const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
+  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
+  const size_t sm = box_smem<TW, TH>(2 * c.post);
+  const bool tma = b.maps && b.maps[l].ok;
+  const BoxMaps maps = tma ? BoxMaps{b.maps[l].post_p, b.maps[l].post_rhs, b.maps[l].post_fl} : BoxMaps{};
+  const float* rhs = l == 0 ? d.div : L.rhs;
+  const float* pin = l == 0 ? b.p_tmp : b.p2 + levels[l].off;
+  float* pout = l == 0 ? d.pa : L.p;
+  const double bytes = 13.0 * cells(L) + 4.0 * cells(C);
+  const char* name = POST_NAMES[l < 7 ? l : 7];
+  if (tma)
+    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, true><<<grid, blk, sm, s>>>(d, L, C, maps, pin, rhs, L.fl, pout, c.post));
+  else
+    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, false><<<grid, blk, sm, s>>>(d, L, C, maps, pin, rhs, L.fl, pout, c.post));
+}
+
+void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
+  set_smem_attrs();
+  const int k = multigrid_first_coarse_level(levels, nl);
+  CoarseSet cs{};
+  cs.n = nl - k;
+  int off = 0;
+  for (int l = k; l < nl; l++) {
+    cs.nx[l - k] = levels[l].nx;
+    cs.ny[l - k] = levels[l].ny;
+    cs.eps[l - k] = levels[l].eps;
+    cs.off[l - k] = off;
+    off += levels[l].nx * levels[l].ny;
+  }
+  cs.rhs_top = b.rhs + levels[k].off;
+  cs.fl_top = b.fluid + levels[k].off;
+  cs.p_out = b.p + levels[k].off;
+  const size_t coarse_smem = (size_t)off * 9 + 16;
+  const double coarse_bytes = 13.0 * levels[k].nx * levels[k].ny;
+  const int cycles = c.cycles < 1 ? 1 : c.cycles;
+  for (int cy = 0; cy < cycles; cy++) {
+    for (int l = 0; l < k; l++) {
+      if (small_tiles(levels[l])) launch_pre<32, 16>(d, levels, l, b, c, s);
+      else launch_pre<64, 32>(d, levels, l, b, c, s);
+    }
+    if (k == 0)
+      RB_LAUNCH("mg_coarse_vcycle", coarse_bytes, s,
+                k_mg_coarse<true><<<1, COARSE_THREADS, coarse_smem, s>>>(d, cs, c.pre, c.post, c.coarse));
+    else
+      RB_LAUNCH("mg_coarse_vcycle", coarse_bytes, s,
+                k_mg_coarse<false><<<1, COARSE_THREADS, coarse_smem, s>>>(d, cs, c.pre, c.post, c.coarse));
+    for (int l = k - 1; l >= 0; l--) {
+      if (small_tiles(levels[l])) launch_post<32, 16>(d, levels, l, b, c, s);
+      else launch_post<64, 32>(d, levels, l, b, c, s);
+    }
   }
 }
 

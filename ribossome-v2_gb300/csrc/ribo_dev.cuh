@@ -86,7 +86,8 @@ struct Dev {
   uint32_t* agg_act;
   uint32_t* agg_nb;
   // fluid-resolution buffers
-  uint8_t* mask;  // 1 = wall
+  uint8_t* mask;    // 1 = wall
+  float2* normal;   // outward wall normal of each fluid cell (from the mask)
   float2* va;     // velocity_a
   float2* vb;     // velocity_b
   float2* vsmooth;
@@ -102,7 +103,9 @@ struct Dev {
   float2* forces;
   const float2* heat;
   float* net_flux;
-  uint32_t* ledger;  // 12 words
+  uint32_t* ledger;   // 12 words
+  uint8_t* fluid0;    // level-0 water flags of the multigrid (1 = water), rebuilt with the mask
+  uint32_t* status;   // error bits written by kernels instead of trapping (RIBO_ERR_*)
 };
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
@@ -208,8 +211,10 @@ __device__ __forceinline__ float2 reflect_n(float2 n, float2 v_in) {
   if (len2(n) > (float)1e-6 && dd < 0.0f) return sub2(v_in, mul2(n, dd));
   return v_in;
 }
+// The wall normal depends on the mask alone, so it is computed once per
+// mask build (k_wall_normals) and read here: same function, same bits.
 __device__ __forceinline__ float2 reflect_if_into_solid(const Dev& d, uint32_t x, uint32_t y, float2 v) {
-  return reflect_n(solid_normal(d, x, y), v);
+  return reflect_n(d.normal[(size_t)y * d.fw + x], v);
 }
 // fluid.wgsl:191-194 on an arbitrary input buffer
 __device__ __forceinline__ float2 raw_velocity_cell(const Dev& d, const float2* vin, uint32_t x, uint32_t y) {

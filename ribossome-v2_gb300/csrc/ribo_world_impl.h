@@ -28,6 +28,18 @@ struct KTimer {
   ~KTimer();
 };
 
+uint64_t ktime_launch_count();
+void ktime_add_launches(uint64_t n);
+
+// A captured step sequence and the ping-pong state it leaves.
+struct GraphEntry {
+  std::string key;
+  cudaGraphExec_t exec = nullptr;
+  uint32_t *chem_end = nullptr;
+  float *temp_end = nullptr, *redox_end = nullptr;
+  uint64_t kernels = 0, uses = 0;
+};
+
 struct World {
   ribo_world_cfg cfg{};
   ribo_world_settings st{};
@@ -46,6 +58,7 @@ struct World {
   uint32_t *agg_act = nullptr, *agg_nb = nullptr;
   // fluid resolution
   uint8_t* mask = nullptr;
+  float2* normal = nullptr;
   uint32_t* mask32 = nullptr;
   float2 *va = nullptr, *vb = nullptr, *vsmooth = nullptr;
   float *pa = nullptr, *pb = nullptr, *div = nullptr;
@@ -63,6 +76,8 @@ struct World {
   std::vector<MgLevel> levels;
   size_t mg_total = 0;
   MgBufs mg{};
+  std::vector<MgLevelMaps> mg_maps;
+  uint32_t* status = nullptr;  // kernel error bits (RIBO_ERR_*)
   // per-step parameters: two slots of 64 copies, device + pinned staging
   ribo_sim_params* d_params = nullptr;
   ribo_sim_params* h_params = nullptr;
@@ -87,6 +102,12 @@ struct World {
   ribo_status read(ribo_field f, void* host, size_t bytes);
   ribo_status step(const ribo_sim_params* per_step, uint32_t n);
   ribo_status ledger_read(uint32_t out[12]);
+  ribo_status check_status();
+  // CUDA-graph replay of repeated step sequences
+  std::vector<GraphEntry> graphs;
+  std::vector<std::string> seen_keys;
+  std::string graph_key(const ribo_sim_params* per_step, uint32_t n, int slot) const;
+  ribo_status record_steps_graphed(const ribo_sim_params* per_step, const ribo_sim_params* ds, uint32_t n, int slot);
   ribo_status read_timing(ribo_kernel_timing* out, uint32_t cap, uint32_t* count);
   void record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uint32_t i);
   cudaError_t bind() const;

@@ -302,6 +302,394 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ Dev d, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mover-parallel scatter (same results as k_scatter, bit for bit).
+//
+// A CTA owns a 32x8 tile of cells; warp w owns row w (lane = cell).
+//  A. Each lane runs the per-cell part of transport_scatter (velocity, hop
+//     probabilities, osmotic pressure, Kawasaki acceptance, local reactions)
+//     and leaves its results in shared memory -- including, for each of the
+//     16 cells of its destination window, the accumulator slot a monomer
+//     landing there ends up in: blocking by rock or by a full cell depends
+//     only on the destination, so it is resolved here once per cell instead
+//     of once per monomer.
+//  B. The warp's movers (all cells x channels, ~1000) are split into 32
+//     equal contiguous ranges, one per lane, so every lane does the same
+//     number of mover iterations whatever the per-cell counts are; each
+//     mover adds its unit to its slot of a shared accumulator covering the
+//     tile and a 2-cell ring (destinations beyond the ring, only with
+//     displacements of more than a cell, go straight to global atomics).
+//  C. The accumulator is added to chem_next with one atomic per non-zero
+//     word.
+namespace st {
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int HALO = 2, AW = TX + 2 * HALO, AH = TY + 2 * HALO, AC = AW * AH;
+constexpr uint16_t FAR = 0xFFFFu;  // destination outside the accumulator
+
+struct Smem {
+  // per cell (index = warp * 32 + lane)
+  float dispx[NT], dispy[NT];
+  int basex[NT], basey[NT];
+  float p_diff[NT], p_settle[NT], p_bound[NT], bsx[NT], bsy[NT], dlen[NT];
+  float press[4][NT], acc[4][NT], accs[4][NT];
+  uint32_t actn[4][NT];            // activated after the local reactions, per channel
+  uint16_t slot[16][NT];           // accumulator slot of each window bin (blocking resolved), or FAR
+  uint32_t off[TY][4 * TX + 1];    // per warp: exclusive prefix of movers over (cell, channel)
+  uint32_t accum[AC][4];           // tile + ring destination sums [cell][channel]
+  uint8_t rock[AC], full[AC];
+  float2 lattice[4][4];            // smooth_start lattice values of this tile
+  float2 jit, glob;                // smooth_start per-step jitter and offset
+};
+}  // namespace st
+
+__global__ void __launch_bounds__(st::NT, 3) k_scatter_tiled(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  st::Smem& S = *reinterpret_cast<st::Smem*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int X0 = blockIdx.x * st::TX, Y0 = blockIdx.y * st::TY;
+  const uint32_t G = d.gw, GH = d.gh;
+
+  // ---- zero the accumulator, load the blocking flags of tile + ring ----
+  for (int e = tid; e < st::AC; e += st::NT) {
+    S.accum[e][0] = S.accum[e][1] = S.accum[e][2] = S.accum[e][3] = 0u;
+    int gx = X0 - st::HALO + e % st::AW, gy = Y0 - st::HALO + e / st::AW;
+    uint8_t rock = 0, full = 0;
+    if (gx >= 0 && gy >= 0 && gx < (int)G && gy < (int)GH) {
+      size_t t = (size_t)gy * G + gx;
+      uint32_t g = __ldg(d.gamma + t);
+      rock = g >= GAMMA_SOLID;
+      full = cell_total4(load_cell(d.chem, t)) > capacity_of(g);
+    }
+    S.rock[e] = rock;
+    S.full[e] = full;
+  }
+  // smooth_start (transport.wgsl:95-117): the per-step jitter and offset and
+  // the lattice values this tile can touch are computed once per CTA.
+  if (tid == 0) {
+    rb_u4 j = rb_pcg4d(0x85EBCA6Bu, P->epoch, RB_S_MOVE + MAX_MOVERS_PER_CH + 2u, P->seed);
+    S.jit = f2(rb_u2f(j.x), rb_u2f(j.y));
+    rb_u4 g = rb_pcg4d(0x9E3779B9u, P->epoch, RB_S_MOVE + MAX_MOVERS_PER_CH, P->seed);
+    S.glob = f2(rb_u2f(g.x), rb_u2f(g.y));
+  }
+  __syncthreads();
+  const uint32_t jx = rb_f2u(S.jit.x * (float)SMOOTH_CELL), jy = rb_f2u(S.jit.y * (float)SMOOTH_CELL);
+  const uint32_t lgx0 = ((uint32_t)X0 + jx) / SMOOTH_CELL, lgy0 = ((uint32_t)Y0 + jy) / SMOOTH_CELL;
+  if (tid < 16) {
+    uint32_t ix = lgx0 + (tid & 3), iy = lgy0 + (tid >> 2);
+    rb_u4 r = rb_pcg4d((ix * 73856093u) ^ (iy * 19349663u), P->epoch, RB_S_MOVE + MAX_MOVERS_PER_CH + 1u, P->seed);
+    S.lattice[tid >> 2][tid & 3] = f2(rb_u2f(r.x), rb_u2f(r.y));
+  }
+  __syncthreads();
+
+  // ---- A. per-cell part (transport.wgsl:120-304) ----
+  const uint32_t x = X0 + lane, y = Y0 + warp;
+  uint32_t mov[4] = {0u, 0u, 0u, 0u};
+  const int sax = lane + st::HALO, say = warp + st::HALO;  // own accumulator cell
+  if (x < G && y < GH) {
+    const size_t idx = (size_t)y * G + x;
+    const uint4 cw = load_cell(d.chem, idx);
+    const uint32_t src_total = cell_total4(cw);
+    if (src_total != 0u) {
+      const uint32_t g_src = __ldg(d.gamma + idx);
+      float2 v = f2(0.0f, 0.0f);
+      if (P->fluid_enabled != 0u && g_src < GAMMA_SOLID) {
+        float2 c = mul2(f2((float)x + 0.5f, (float)y + 0.5f), d.cell_w);
+        float2 v0 = fluid_velocity_at_world(d, c);
+        float h = rb_max(P->dt, 0.0f);
+        float2 c2 = f2(c.x + v0.x * d.wpf_x * h * 0.5f, c.y + v0.y * d.wpf_y * h * 0.5f);
+        v = fluid_velocity_at_world(d, c2);
+      }
+      if (v.x != 0.0f || v.y != 0.0f) {
+        bool rock_r = x + 1u < G && S.rock[say * st::AW + sax + 1];
+        bool rock_l = x > 0u && S.rock[say * st::AW + sax - 1];
+        bool rock_u = y + 1u < GH && S.rock[(say + 1) * st::AW + sax];
+        bool rock_d = y > 0u && S.rock[(say - 1) * st::AW + sax];
+        if ((v.x > 0.0f && rock_r) || (v.x < 0.0f && rock_l)) v.x = 0.0f;
+        else if ((v.x > 0.0f && rock_l) || (v.x < 0.0f && rock_r)) v.x *= 0.5f;
+        if ((v.y > 0.0f && rock_u) || (v.y < 0.0f && rock_d)) v.y = 0.0f;
+        else if ((v.y > 0.0f && rock_d) || (v.y < 0.0f && rock_u)) v.y *= 0.5f;
+      }
+      const float tn = (float)(P->transport_every > 1u ? P->transport_every : 1u);
+      const float dtp = rb_max(P->dt, 0.0f);
+      float2 disp = f2(v.x * d.sx * dtp * tn, v.y * d.sy * dtp * tn);
+      float agitation = rb_clamp(len2(v) / DIFF_AGITATION_SPEED, 0.0f, 1.0f);
+      float p_diff = rb_clamp(DIFF_HOP_P * rb_mix(DIFF_HOP_FLOOR, 1.0f, agitation) * rb_max(P->diffusion, 0.0f) * tn, 0.0f, 0.5f);
+      if (g_src > 0u) p_diff = rb_min(DIFF_HOP_P * BURIED_DIFF_FACTOR / (1.0f + GAMMA_POROSITY_K * (float)g_src) * tn, 0.5f);
+      const uint32_t cap_self = capacity_of(g_src);
+      if (src_total > cap_self) p_diff = rb_min(CHEM_SQUEEZE_P * tn, 0.5f);
+      float p_settle = 0.0f;
+      if (g_src == 0u) p_settle = rb_min(MONOMER_SETTLE_P * rb_max(P->settle, 0.0f) * tn, 0.5f);
+      float press[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+      float max_drop = 0.0f;
+      if (P->monomer_pressure > 0.0f) {
+        float f_self = (float)src_total / (float)(cap_self > 1u ? cap_self : 1u);
+        long nb[4] = {1, -1, (long)G, -(long)G};
+        bool inside[4] = {x + 1u < G, x > 0u, y + 1u < GH, y > 0u};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          if (!inside[k]) continue;
+          size_t n = (size_t)((long)idx + nb[k]);
+          uint32_t cap_n = capacity_of(__ldg(d.gamma + n));
+          if (cap_n == 0u) continue;
+          float f_n = (float)cell_total4(load_cell(d.chem, n)) / (float)cap_n;
+          press[k] = rb_max((float)0.05, 1.0f + P->monomer_pressure * (f_self - f_n));
+          max_drop = rb_max(max_drop, f_self - f_n);
+        }
+      }
+      p_diff = rb_clamp(p_diff + PRESSURE_HOP_P * P->monomer_pressure * max_drop * tn, 0.0f, 0.5f);
+      const float light_t = d.light[(size_t)(umin(y, GH - 1u) / LIGHT_DIV) * d.lw + umin(x, G - 1u) / LIGHT_DIV];
+      float p_bound = 0.0f;
+      float acc[4] = {1.0f, 1.0f, 1.0f, 1.0f}, accs[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+      if (P->aggregation > 0.0f && src_total <= cap_self) {
+        float e[5];
+        e[0] = (float)(d.agg_nb[idx] + d.agg_act[idx]);
+        e[1] = x + 1u < G ? (float)(d.agg_nb[idx + 1] + d.agg_act[idx + 1]) : 0.0f;
+        e[2] = x > 0u ? (float)(d.agg_nb[idx - 1] + d.agg_act[idx - 1]) : 0.0f;
+        e[3] = y + 1u < GH ? (float)(d.agg_nb[idx + G] + d.agg_act[idx + G]) : 0.0f;
+        e[4] = y > 0u ? (float)(d.agg_nb[idx - G] + d.agg_act[idx - G]) : 0.0f;
+        uint32_t fx = umin((x * (uint32_t)d.fw) / G, (uint32_t)d.fw - 1u);
+        uint32_t fy = umin((y * (uint32_t)d.fh) / GH, (uint32_t)d.fh - 1u);
+        float t_rel = 1.0f + rb_max(d.temp_in[(size_t)fy * d.fw + fx], 0.0f) / TEMP_ACT_THRESHOLD;
+        float room = rb_clamp(5.0f * (1.0f - (float)src_total / (float)(cap_self > 1u ? cap_self : 1u)), 0.0f, 1.0f);
+        float k_e = P->aggregation * room / t_rel;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          float drop = e[0] - e[k + 1];
+          if (drop > 0.0f) acc[k] = rb_exp(-k_e * drop);
+          float rise = e[k + 1] - e[0];
+          if (rise > 0.0f) accs[k] = rb_exp(-k_e * rise);
+        }
+        p_bound = 1.0f - rb_exp(-k_e * rb_min(rb_max(e[0] - 1.0f, 0.0f), 48.0f));
+      }
+      float2 bound_start = f2(0.0f, 0.0f);
+      if (p_bound > 0.0f) {  // smooth_start(x, y) from the tile's lattice
+        const uint32_t sx = x + jx, sy = y + jy;
+        const uint32_t lx = sx / SMOOTH_CELL - lgx0, ly = sy / SMOOTH_CELL - lgy0;
+        float tx = rb_smoothstep01(((float)(sx % SMOOTH_CELL) + 0.5f) / (float)SMOOTH_CELL);
+        float ty = rb_smoothstep01(((float)(sy % SMOOTH_CELL) + 0.5f) / (float)SMOOTH_CELL);
+        float2 n = mix2(mix2(S.lattice[ly][lx], S.lattice[ly][lx + 1], tx), mix2(S.lattice[ly + 1][lx], S.lattice[ly + 1][lx + 1], tx), ty);
+        float vx = rb_fract(n.x + S.glob.x), vy = rb_fract(n.y + S.glob.y);
+        bound_start = f2(1.0f - rb_abs(2.0f * vx - 1.0f), 1.0f - rb_abs(2.0f * vy - 1.0f));
+      }
+      const bool disperse = g_src > 0u && (disp.x != 0.0f || disp.y != 0.0f);
+      const int basex = rb_f2i(rb_floor(disp.x)) - 1, basey = rb_f2i(rb_floor(disp.y)) - 1;
+      S.dispx[tid] = disp.x;
+      S.dispy[tid] = disp.y;
+      S.basex[tid] = basex;
+      S.basey[tid] = basey;
+      S.p_diff[tid] = p_diff;
+      S.p_settle[tid] = p_settle;
+      S.p_bound[tid] = p_bound;
+      S.bsx[tid] = bound_start.x;
+      S.bsy[tid] = bound_start.y;
+      S.dlen[tid] = disperse ? len2(disp) : -1.0f;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        S.press[k][tid] = press[k];
+        S.acc[k][tid] = acc[k];
+        S.accs[k][tid] = accs[k];
+      }
+      // destination slot of every window bin (transport.wgsl:364-401)
+#pragma unroll 4
+      for (int b = 0; b < 16; b++) {
+        int tx = iclamp((int)x + basex + (b & 3), 0, (int)G - 1);
+        int ty = iclamp((int)y + basey + (b >> 2), 0, (int)GH - 1);
+        int ax = tx - (X0 - st::HALO), ay = ty - (Y0 - st::HALO);
+        const bool near = ax >= 0 && ax < st::AW && ay >= 0 && ay < st::AH;
+        uint16_t sl;
+        if (tx == (int)x && ty == (int)y) {
+          sl = (uint16_t)(say * st::AW + sax);
+        } else {
+          bool rock, full;
+          if (near) {
+            rock = S.rock[ay * st::AW + ax];
+            full = S.full[ay * st::AW + ax];
+          } else {
+            size_t t = (size_t)ty * G + tx;
+            uint32_t g_t = __ldg(d.gamma + t);
+            rock = g_t >= GAMMA_SOLID;
+            full = cell_total4(load_cell(d.chem, t)) > capacity_of(g_t);
+          }
+          const bool blocked = rock ? (g_src < GAMMA_SOLID) : full;
+          sl = blocked ? (uint16_t)(say * st::AW + sax) : (near ? (uint16_t)(ay * st::AW + ax) : st::FAR);
+        }
+        S.slot[b][tid] = sl;
+      }
+      // local reactions per channel (transport.wgsl:262-294)
+      const uint32_t words[4] = {cw.x, cw.y, cw.z, cw.w};
+#pragma unroll
+      for (uint32_t ch = 0; ch < 4; ch++) {
+        const uint32_t slot = (uint32_t)(idx * 4 + ch);
+        uint32_t act_n = words[ch] & CHEM_STATE_MASK;
+        uint32_t spent_n = words[ch] >> 16;
+        S.actn[ch][tid] = 0u;
+        if (act_n + spent_n == 0u) continue;
+        if (spent_n > 0u) {
+          float sens = 1.0f + CHEM_SENSITIZE * (float)umin(act_n, 8u);
+          float exp_act = (float)umin(spent_n, 8u) * tn *
+                          (LIGHT_ACT_P * rb_max(P->uv_strength, 0.0f) * rb_max(P->direct_photoactivation, 0.0f) * light_t * sens +
+                           rb_max(P->reactivation_rate, 0.0f));
+          uint32_t na = rb_f2u(rb_floor(exp_act));
+          float frac = exp_act - (float)na;
+          if (frac > 0.0f && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_PHOTO, P->seed).x) < frac) na += 1u;
+          na = umin(na, umin(spent_n, 8u));
+          act_n += na;
+          spent_n -= na;
+        }
+        if (act_n > 0u) {
+          float shield = 1.0f / (1.0f + CHEM_SHIELD * (float)(umin(act_n, 8u) - 1u));
+          float exp_dec = (float)umin(act_n, 8u) * rb_max(P->activation_decay, 0.0f) * shield * tn;
+          if (exp_dec > 0.0f && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_DECAY, P->seed).x) < exp_dec) {
+            act_n -= 1u;
+            spent_n += 1u;
+          }
+        }
+        const uint32_t n = act_n + spent_n;
+        const uint32_t movers = umin(n, MAX_MOVERS_PER_CH);
+        const uint32_t act_stay = act_n - umin(act_n, movers);
+        const uint32_t stay = act_stay + (n - movers - act_stay) * CHEM_SPENT_ONE;
+        if (stay) atomicAdd(&S.accum[say * st::AW + sax][ch], stay);
+        S.actn[ch][tid] = act_n;
+        mov[ch] = movers;
+      }
+    }
+  }
+
+  // ---- B. movers, split evenly over the lanes of the warp ----
+  uint32_t cell_sum = mov[0] + mov[1] + mov[2] + mov[3];
+  uint32_t incl = cell_sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  {
+    uint32_t base = incl - cell_sum;
+    uint32_t* off = S.off[warp];
+    off[lane * 4 + 0] = base;
+    off[lane * 4 + 1] = base + mov[0];
+    off[lane * 4 + 2] = base + mov[0] + mov[1];
+    off[lane * 4 + 3] = base + mov[0] + mov[1] + mov[2];
+    if (lane == 31) off[128] = total;
+  }
+  __syncthreads();
+
+  const uint32_t chunk = (total + 31u) / 32u;
+  uint32_t j = umin(total, lane * chunk);
+  const uint32_t j_end = umin(total, j + chunk);
+  if (j < j_end) {
+    const uint32_t* off = S.off[warp];
+    int lo = 0, hi = 127;  // segment s with off[s] <= j < off[s+1] (the largest such s)
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (off[mid] <= j) lo = mid;
+      else hi = mid - 1;
+    }
+    int s = lo;
+    uint32_t k = j - off[s];
+    uint32_t seg_end = off[s + 1];
+    int c = s >> 2, ch = s & 3;
+    int ct = warp * 32 + c;
+    const int cy = Y0 + warp;
+    int cx = X0 + c;
+    uint32_t slot = (uint32_t)(((size_t)cy * G + cx) * 4 + ch);
+    uint32_t act_n = S.actn[ch][ct];
+    float dispx = S.dispx[ct], dispy = S.dispy[ct], p_diff = S.p_diff[ct], p_settle = S.p_settle[ct];
+    float p_bound = S.p_bound[ct], bsx = S.bsx[ct], bsy = S.bsy[ct], dlen = S.dlen[ct];
+    int basex = S.basex[ct], basey = S.basey[ct];
+    const uint32_t epoch = P->epoch, seed = P->seed;
+    const float cohesion = P->cohesion;
+    for (; j < j_end; j++) {
+      if (j >= seg_end) {  // next non-empty segment
+        do {
+          s++;
+          seg_end = off[s + 1];
+        } while (j >= seg_end);
+        k = j - off[s];
+        c = s >> 2;
+        ch = s & 3;
+        ct = warp * 32 + c;
+        cx = X0 + c;
+        slot = (uint32_t)(((size_t)cy * G + cx) * 4 + ch);
+        act_n = S.actn[ch][ct];
+        dispx = S.dispx[ct];
+        dispy = S.dispy[ct];
+        p_diff = S.p_diff[ct];
+        p_settle = S.p_settle[ct];
+        p_bound = S.p_bound[ct];
+        bsx = S.bsx[ct];
+        bsy = S.bsy[ct];
+        dlen = S.dlen[ct];
+        basex = S.basex[ct];
+        basey = S.basey[ct];
+      }
+      const bool is_act = k < act_n;
+      const uint32_t unit = is_act ? 1u : CHEM_SPENT_ONE;
+      rb_u4 ru = rb_pcg4d(slot, epoch, RB_S_MOVE + k, seed);
+      float rfx = rb_u2f(ru.x), rfy = rb_u2f(ru.y), rfz = rb_u2f(ru.z), rfw = rb_u2f(ru.w);
+      bool bound = is_act && p_bound > 0.0f && rb_fract(rfz * (float)7.31 + rfw * (float)3.17) < p_bound;
+      float px = (bound ? bsx : rfx) + dispx;
+      float py = (bound ? bsy : rfy) + dispy;
+      if (dlen >= 0.0f) {
+        rb_u4 rj = rb_pcg4d(slot, epoch, RB_S_DISPERSE + k, seed);
+        float jxx = (rb_u2f(rj.x) * 2.0f - 1.0f) * dlen * RUBBLE_DISPERSION;
+        float jyy = (rb_u2f(rj.y) * 2.0f - 1.0f) * dlen * RUBBLE_DISPERSION;
+        px += rb_clamp(jxx, (float)-0.9, (float)0.9);
+        py += rb_clamp(jyy, (float)-0.9, (float)0.9);
+      }
+      if (rfz < p_diff) {
+        float w0 = S.press[0][ct], w1 = S.press[1][ct], w2 = S.press[2][ct], w3 = S.press[3][ct];
+        if (is_act && cohesion > 0.0f) {
+          // cohesion weights (transport.wgsl:298-304), only needed on a hop
+          const size_t ci = (size_t)cy * G + cx;
+          if ((uint32_t)cx + 1u < G) w0 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci + 1) * 4 + ch) & CHEM_STATE_MASK, 8u);
+          if (cx > 0) w1 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci - 1) * 4 + ch) & CHEM_STATE_MASK, 8u);
+          if ((uint32_t)cy + 1u < GH) w2 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci + G) * 4 + ch) & CHEM_STATE_MASK, 8u);
+          if (cy > 0) w3 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci - G) * 4 + ch) & CHEM_STATE_MASK, 8u);
+        }
+        float u = rfw * (w0 + w1 + w2 + w3);
+        uint32_t dd;
+        if (u < w0) dd = 0u;
+        else if ((u -= w0) < w1) dd = 1u;
+        else if ((u -= w1) < w2) dd = 2u;
+        else dd = 3u;
+        float acc_d = is_act ? S.acc[dd][ct] : S.accs[dd][ct];
+        bool stay_put = rb_fract(rfw * (float)13.73 + rfx * (float)5.31) >= acc_d;
+        if (!stay_put) {
+          if (dd == 0u) px += 1.0f;
+          else if (dd == 1u) px -= 1.0f;
+          else if (dd == 2u) py += 1.0f;
+          else py -= 1.0f;
+        }
+      } else if (rfz < p_diff + p_settle) {
+        py -= 1.0f;
+      }
+      const int offx = rb_f2i(rb_floor(px)) - basex, offy = rb_f2i(rb_floor(py)) - basey;
+      const uint32_t bi = (uint32_t)iclamp(offy, 0, 3) * 4u + (uint32_t)iclamp(offx, 0, 3);
+      const uint16_t sl = S.slot[bi][ct];
+      if (sl != st::FAR) {
+        atomicAdd(&S.accum[sl][ch], unit);
+      } else {
+        int tx = iclamp(cx + basex + (int)(bi & 3u), 0, (int)G - 1);
+        int ty = iclamp(cy + basey + (int)(bi >> 2), 0, (int)GH - 1);
+        atomicAdd(d.chem_next + ((size_t)ty * G + tx) * 4 + ch, unit);
+      }
+      k++;
+    }
+  }
+  __syncthreads();
+
+  // ---- C. accumulator -> chem_next ----
+  for (int e = tid; e < st::AC * 4; e += st::NT) {
+    int cell = e >> 2, ch = e & 3;
+    uint32_t v = S.accum[cell][ch];
+    if (!v) continue;
+    int gx = X0 - st::HALO + cell % st::AW, gy = Y0 - st::HALO + cell / st::AW;
+    atomicAdd(d.chem_next + ((size_t)gy * G + gx) * 4 + ch, v);
+  }
+}
+
 // ledger.wgsl:225-245: per-block sums in registers and warp shuffles, then
 // one global atomic add per counter (u32, wrapping like the reference).
 __global__ void __launch_bounds__(256) k_ledger(const uint32_t* __restrict__ chem, size_t cells, uint32_t* out) {
@@ -349,8 +737,21 @@ void launch_agg(const Dev& d, cudaStream_t s) {
   RB_LAUNCH("agg_count", 20.0 * gc(d), s, k_agg_count<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d));
   RB_LAUNCH("agg_neighbours", 8.0 * gc(d), s, k_agg_neighbours<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d));
 }
-void launch_scatter(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
-  RB_LAUNCH("transport_scatter", 45.0 * gc(d) + 12.0 * fc(d), s, k_scatter<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, P));
+void launch_scatter(const Dev& d, const ribo_sim_params* P, bool simple, cudaStream_t s) {
+  const double bytes = 45.0 * gc(d) + 12.0 * fc(d);
+  if (simple) {
+    RB_LAUNCH("transport_scatter_simple", bytes, s, k_scatter<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, P));
+    return;
+  }
+  static uint64_t attr_done = 0;  // one bit per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!(attr_done >> (dev & 63) & 1ull)) {
+    cudaFuncSetAttribute(k_scatter_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(st::Smem));
+    attr_done |= 1ull << (dev & 63);
+  }
+  dim3 grid((d.gw + st::TX - 1) / st::TX, (d.gh + st::TY - 1) / st::TY);
+  RB_LAUNCH("transport_scatter", bytes, s, k_scatter_tiled<<<grid, st::NT, sizeof(st::Smem), s>>>(d, P));
 }
 void launch_ledger(const Dev& d, const uint32_t* chem, uint32_t* out12, cudaStream_t s) {
   cudaMemsetAsync(out12, 0, 12 * sizeof(uint32_t), s);

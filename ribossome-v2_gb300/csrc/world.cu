@@ -70,6 +70,9 @@ void ktime_end(cudaStream_t s) {
   cudaEventRecord(t->recs.back().b, s);
 }
 
+uint64_t ktime_launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void ktime_add_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 cudaEvent_t KTimer::event() {
   if (used == pool.size()) {
     cudaEvent_t e;
@@ -154,6 +157,7 @@ Dev World::dev() const {
   d.agg_act = agg_act;
   d.agg_nb = agg_nb;
   d.mask = mask;
+  d.normal = normal;
   d.va = va;
   d.vb = vb;
   d.vsmooth = vsmooth;
@@ -170,6 +174,8 @@ Dev World::dev() const {
   d.heat = heat;
   d.net_flux = net_flux;
   d.ledger = ledger;
+  d.fluid0 = (mg.fluid && !levels.empty()) ? mg.fluid + levels[0].off : nullptr;
+  d.status = status;
   return d;
 }
 
@@ -209,6 +215,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(agg_act, C * 4);
   RB_ALLOC(agg_nb, C * 4);
   RB_ALLOC(mask, F);
+  RB_ALLOC(normal, F * 8);
   RB_ALLOC(va, F * 8);
   RB_ALLOC(vb, F * 8);
   RB_ALLOC(vsmooth, F * 8);
@@ -242,7 +249,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
     size_t off = 0;
     for (;;) {
       levels.push_back(MgLevel{nx, ny, off, (float)1e-4 * (float)(1u << l)});
-      off += (size_t)nx * ny;
+      off += ((size_t)nx * ny + 63) & ~(size_t)63;  // 64-element aligned level bases (TMA wants 16-byte bases)
       if ((uint32_t)nx > cfg.mg_min_size && (uint32_t)ny > cfg.mg_min_size && nx % 2 == 0 && ny % 2 == 0) {
         nx /= 2;
         ny /= 2;
@@ -257,6 +264,8 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(mg.rhs, mg_total * 4);
   RB_ALLOC(mg.fluid, mg_total);
   RB_ALLOC(mg.p_tmp, F * 4);
+  RB_ALLOC(mg.p2, mg_total * 4);
+  RB_ALLOC(status, 16);
   RB_ALLOC(d_params, 2 * MAX_STEPS * sizeof(ribo_sim_params));
 #undef RB_ALLOC
   RB_TRY(cudaMallocHost((void**)&h_params, 2 * MAX_STEPS * sizeof(ribo_sim_params)), "pinned params");
@@ -266,6 +275,13 @@ ribo_status World::init(const ribo_world_cfg& c) {
   for (int k = 0; k < 8; k++) RB_TRY(cudaEventCreate(&marks[k]), "event");
   // gamma = 0 at creation: derive slope and mask once.
   Dev d = dev();
+  {
+    MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, 1};
+    mg_maps.assign(levels.size(), MgLevelMaps{});
+    if (multigrid_fused_ok(levels.data(), (int)levels.size(), c))
+      multigrid_make_maps(levels.data(), (int)levels.size(), c, mg, d, mg_maps.data());
+    mg.maps = mg_maps.data();
+  }
   launch_slope(d, (float)cfg.world_units_per_cell, stream);
   launch_solid_mask(d, stream);
   RB_TRY(cudaGetLastError(), "init kernels");
@@ -275,6 +291,8 @@ ribo_status World::init(const ribo_world_cfg& c) {
 
 World::~World() {
   if (stream) cudaStreamSynchronize(stream);
+  for (GraphEntry& g : graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   for (void* p : allocs) cudaFree(p);
   if (h_params) cudaFreeHost(h_params);
   for (int k = 0; k < 2; k++)
@@ -329,6 +347,10 @@ ribo_status World::read(ribo_field f, void* host, size_t bytes) {
   }
   RB_TRY(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, stream), "read");
   RB_TRY(cudaStreamSynchronize(stream), "read");
+  {
+    ribo_status s = check_status();
+    if (s != RIBO_OK) return s;
+  }
   return RIBO_OK;
 }
 
@@ -336,7 +358,10 @@ ribo_status World::read(ribo_field f, void* host, size_t bytes) {
 void World::pressure_solve(const Dev& d) {
   if (st.multigrid) {
     MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, (int)(st.mg_cycles < 1 ? 1 : st.mg_cycles)};
-    launch_multigrid(d, levels.data(), (int)levels.size(), mg, c, stream);
+    if (!st.mg_unfused && multigrid_fused_ok(levels.data(), (int)levels.size(), c))
+      launch_multigrid_fused(d, levels.data(), (int)levels.size(), mg, c, stream);
+    else
+      launch_multigrid(d, levels.data(), (int)levels.size(), mg, c, stream);
   } else {
     uint32_t it = st.jacobi_iters < 2 ? 2 : (st.jacobi_iters > 128 ? 128 : st.jacobi_iters);
     it = (it + 1u) & ~1u;
@@ -370,7 +395,7 @@ void World::record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uin
   if (hp.epoch % te == 0u) {
     Dev d = dev();
     if (hp.aggregation > 0.0f) launch_agg(d, stream);
-    launch_scatter(d, P, stream);
+    launch_scatter(d, P, st.transport_simple != 0, stream);
     std::swap(chem_cur, chem_nxt);  // transport_commit
     cudaMemsetAsync(chem_nxt, 0, cells() * 16, stream);
   }
@@ -402,12 +427,93 @@ ribo_status World::step(const ribo_sim_params* per_step, uint32_t n) {
     timer.recs.clear();
     timer.used = 0;
     g_active_timer = &timer;
+    for (uint32_t i = 0; i < n; i++) record_step(per_step[i], ds + i, i);
+    g_active_timer = nullptr;
+  } else {
+    ribo_status s = record_steps_graphed(per_step, ds, n, slot);
+    if (s != RIBO_OK) return s;
   }
-  for (uint32_t i = 0; i < n; i++) record_step(per_step[i], ds + i, i);
   last_steps = n;
-  g_active_timer = nullptr;
   RB_TRY(cudaGetLastError(), "step launch");
   RB_TRY(cudaEventRecord(t1, stream), "event");
+  return RIBO_OK;
+}
+
+// Repeated step sequences replay from CUDA graphs.  The kernels of a call
+// depend only on the per-step schedule (which blocks run), the settings,
+// the parameter slot and the ping-pong state of chem / temperature / redox,
+// so those form the key; a sequence is captured the second time its key is
+// seen and replayed afterwards, with the host ping-pong state moved to the
+// state the capture left.
+std::string World::graph_key(const ribo_sim_params* per_step, uint32_t n, int slot) const {
+  std::string k;
+  k.reserve(64 + n);
+  auto put = [&](const void* p, size_t b) { k.append(reinterpret_cast<const char*>(p), b); };
+  put(&n, 4);
+  put(&slot, 4);
+  put(&st, sizeof st);
+  put(&chem_cur, sizeof(void*));
+  put(&temp_cur, sizeof(void*));
+  put(&redox_cur, sizeof(void*));
+  uint32_t substep = st.fluid_substep < 1 ? 1 : (st.fluid_substep > 4 ? 4 : st.fluid_substep);
+  for (uint32_t i = 0; i < n; i++) {
+    const ribo_sim_params& p = per_step[i];
+    uint32_t te = p.transport_every < 1 ? 1 : p.transport_every;
+    char c = (char)((st.fluid_enabled && p.epoch % substep == 0u ? 1 : 0) | (p.epoch % te == 0u ? 2 : 0) |
+                    (p.aggregation > 0.0f ? 4 : 0));
+    k.push_back(c);
+  }
+  return k;
+}
+
+ribo_status World::record_steps_graphed(const ribo_sim_params* per_step, const ribo_sim_params* ds, uint32_t n, int slot) {
+  if (cfg.no_graphs) {
+    for (uint32_t i = 0; i < n; i++) record_step(per_step[i], ds + i, i);
+    return RIBO_OK;
+  }
+  std::string key = graph_key(per_step, n, slot);
+  for (GraphEntry& g : graphs) {
+    if (g.key != key) continue;
+    RB_TRY(cudaGraphLaunch(g.exec, stream), "graph launch");
+    chem_cur = g.chem_end;
+    chem_nxt = g.chem_end == chem_a ? chem_b : chem_a;
+    temp_cur = g.temp_end;
+    temp_nxt = g.temp_end == temp_a ? temp_b : temp_a;
+    redox_cur = g.redox_end;
+    redox_nxt = g.redox_end == redox_a ? redox_b : redox_a;
+    ktime_add_launches(g.kernels);
+    g.uses++;
+    return RIBO_OK;
+  }
+  bool seen = false;
+  for (const std::string& s : seen_keys) seen = seen || s == key;
+  if (!seen) {
+    if (seen_keys.size() >= 16) seen_keys.erase(seen_keys.begin());
+    seen_keys.push_back(key);
+    for (uint32_t i = 0; i < n; i++) record_step(per_step[i], ds + i, i);
+    return RIBO_OK;
+  }
+  // capture
+  uint64_t l0 = ktime_launch_count();
+  RB_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capture");
+  for (uint32_t i = 0; i < n; i++) record_step(per_step[i], ds + i, i);
+  cudaGraph_t graph = nullptr;
+  RB_TRY(cudaStreamEndCapture(stream, &graph), "capture");
+  GraphEntry e;
+  e.key = key;
+  e.kernels = ktime_launch_count() - l0;
+  cudaError_t err = cudaGraphInstantiate(&e.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  RB_TRY(err, "graph instantiate");
+  e.chem_end = chem_cur;
+  e.temp_end = temp_cur;
+  e.redox_end = redox_cur;
+  RB_TRY(cudaGraphLaunch(e.exec, stream), "graph launch");
+  if (graphs.size() >= 8) {
+    cudaGraphExecDestroy(graphs.front().exec);
+    graphs.erase(graphs.begin());
+  }
+  graphs.push_back(e);
   return RIBO_OK;
 }
 
@@ -438,12 +544,29 @@ ribo_status World::read_timing(ribo_kernel_timing* out, uint32_t cap, uint32_t* 
   return RIBO_OK;
 }
 
+// Kernel-side failures (a bounded wait that ran out) are reported through
+// the status word rather than by trapping; it is read at every host sync.
+ribo_status World::check_status() {
+  uint32_t h = 0;
+  RB_TRY(cudaMemcpyAsync(&h, status, 4, cudaMemcpyDeviceToHost, stream), "status");
+  RB_TRY(cudaStreamSynchronize(stream), "status");
+  if (h) {
+    RB_TRY(cudaMemsetAsync(status, 0, 4, stream), "status");
+    return set_error(RIBO_TIMEOUT, "a kernel wait timed out (status 0x%x); results of the last steps are invalid", h);
+  }
+  return RIBO_OK;
+}
+
 ribo_status World::ledger_read(uint32_t out[12]) {
   RB_TRY(bind(), "device");
   launch_ledger(dev(), chem_cur, ledger, stream);
   RB_TRY(cudaGetLastError(), "ledger");
   RB_TRY(cudaMemcpyAsync(out, ledger, 12 * 4, cudaMemcpyDeviceToHost, stream), "ledger");
   RB_TRY(cudaStreamSynchronize(stream), "ledger");
+  {
+    ribo_status s = check_status();
+    if (s != RIBO_OK) return s;
+  }
   return RIBO_OK;
 }
 
@@ -664,7 +787,9 @@ ribo_status ribo_world_elapsed_ms(ribo_world* w, uint32_t a, uint32_t b, float* 
 
 ribo_status ribo_world_sync(ribo_world* w) {
   if (!w) return set_error(RIBO_INVALID_ARG, "null world");
-  return ribo::cuda_status(cudaStreamSynchronize(w->w.stream), "sync");
+  ribo_status st = ribo::cuda_status(cudaStreamSynchronize(w->w.stream), "sync");
+  if (st != RIBO_OK) return st;
+  return w->w.check_status();
 }
 
 ribo_status ribo_world_enable_kernel_timing(ribo_world* w, int enable) {

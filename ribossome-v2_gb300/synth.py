@@ -65,8 +65,9 @@ def value_noise(w: int, h: int, seed: int, octaves: int = 4, base_period: float 
 
 
 def make_world_inputs(grid, fluid=None, seed: int = 1000, rock_frac: float = 0.10, monomer_mean: float = 4.0,
-                      max_disp: float = 0.5, dt: float = 1.0, uv_depth: float = 2.0) -> dict:
-    """Returns {ribo_world field id: numpy array} for a world of the given size."""
+                      max_disp: float = 0.5, dt: float = 1.0, uv_depth: float = 2.0, rubble_frac: float = 0.0) -> dict:
+    """Returns {ribo_world field id: numpy array} for a world of the given size.
+    rubble_frac > 0 turns that fraction of the non-rock cells into rubble (1 or 2 grains)."""
     gw, gh = (grid, grid) if isinstance(grid, int) else grid
     fw, fh = (gw, gh) if fluid is None else ((fluid, fluid) if isinstance(fluid, int) else fluid)
     r = gw // fw
@@ -75,6 +76,10 @@ def make_world_inputs(grid, fluid=None, seed: int = 1000, rock_frac: float = 0.1
     rn = value_noise(gw, gh, seed * 7 + 1, octaves=4, base_period=max(8.0, min(gw, gh) / 8.0))
     thr = np.quantile(rn, 1.0 - rock_frac) if rock_frac > 0 else np.inf
     gamma = np.where(rn > thr, 6, 0).astype(np.uint32)
+    if rubble_frac > 0:
+        rr = rng.random((gh, gw))
+        rub = (rr < rubble_frac) & (gamma == 0)
+        gamma[rub] = np.where(rr[rub] < rubble_frac / 2, 1, 2).astype(np.uint32)
     # monomers: 8 Poisson counts per cell
     counts = rng.poisson(monomer_mean, size=(gh, gw, 4, 2)).astype(np.uint32)
     counts = np.minimum(counts, 0xFFFF)
@@ -95,11 +100,15 @@ def make_world_inputs(grid, fluid=None, seed: int = 1000, rock_frac: float = 0.1
     band0 = np.exp(-uv_depth * depth)[:, None] * np.ones((1, lw))
     band1 = np.exp(-uv_depth * 0.03 * depth)[:, None] * np.ones((1, lw))
     light = np.stack([band0, band1]).astype(np.float32)
+    zf = np.zeros((fh, fw), np.float32)
     return {
         rw.GAMMA: gamma,
         rw.CHEM: chem,
         rw.VELOCITY: vel.astype(np.float32),
         rw.LIGHT: light,
+        rw.PRESSURE: zf,
+        rw.TEMP: zf,
+        rw.REDOX: zf,
     }
 
 

@@ -14,6 +14,17 @@ BASE = dict(dt=1.0, transport_every=1, sun_heat=0.0, day_period=0.0)
 CASES = [
     # id, grid, fluid, params, settings, steps, mg
     ("c0-256-mg5-2x3+3", 256, None, BASE, dict(fluid_substep=1, mg_cycles=2), 6, dict(mg_min_size=16, mg_pre=3, mg_post=3)),
+    ("c0-256-unfused-dispatch", 256, None, BASE, dict(fluid_substep=1, mg_cycles=2, mg_unfused=1), 4,
+     dict(mg_min_size=16, mg_pre=3, mg_post=3)),
+    ("512-reference-mg-constants", 512, None, BASE, dict(fluid_substep=1), 3, {}),
+    ("384-mg-1+4-3cycles", 384, None, BASE, dict(fluid_substep=1, mg_cycles=3), 3, dict(mg_pre=1, mg_post=4, mg_coarse=7)),
+    ("transport-simple-kernel", 128, None, dict(BASE, cohesion=0.7, monomer_pressure=1.0), dict(fluid_substep=1, transport_simple=1),
+     4, dict(rubble_frac=0.2)),
+    ("long-displacement-rubble", 160, 80, dict(BASE, dt=9.0, cohesion=0.7, monomer_pressure=1.0, aggregation=0.1),
+     dict(fluid_substep=1), 4, dict(rubble_frac=0.2, max_disp=2.5, dt=9.0)),
+    ("crowded-cells", 96, None, dict(BASE, settle=2.0), dict(fluid_substep=1), 4, dict(monomer_mean=40.0, rubble_frac=0.1)),
+    # 200 is not a multiple of 16: the fused V-cycle stages its tiles with plain loads instead of TMA
+    ("200-plain-load-tiles", 200, None, BASE, dict(fluid_substep=1, mg_cycles=2), 3, dict(mg_pre=3, mg_post=3)),
     ("test-cfg-256-128-defaults", 256, 128, dict(dt=1.0), {}, 8, {}),
     ("64-reference-constants", 64, None, dict(BASE, diffusion=30.0, settle=1.0, thermal_activation=1.0,
                                               aggregation=0.02), dict(fluid_substep=1), 10, {}),
@@ -50,6 +61,26 @@ def test_steps_bit_exact(rw, ro, case):
         done += batch
         compare_worlds(g, o, f"after {done} steps")
     assert g.ledger_blocking() == o.ledger_blocking()
+
+
+def test_graph_replay_matches_direct_launches(rw, ro):
+    """Repeated step sequences replay from CUDA graphs; the results must equal
+    direct launches and the oracle."""
+    import synth
+
+    inputs = synth.make_world_inputs(128, seed=77, rubble_frac=0.1)
+    worlds = [rw.World(128, seed=77), rw.World(128, seed=77, no_graphs=1)]
+    o = ro.OracleWorld(128, seed=77)
+    for w in worlds + [o]:
+        w.seed_inputs(inputs)
+        for k, v in BASE.items():
+            setattr(w.params, k, v)
+        w.settings.fluid_substep = 1
+    for call in range(6):
+        for w in worlds + [o]:
+            w.encode_steps(3)
+        compare_worlds(worlds[0], o, f"graphs, call {call}")
+        compare_worlds(worlds[1], o, f"direct, call {call}")
 
 
 def test_fluid_disable_clears_once(rw, ro):
