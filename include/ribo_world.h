@@ -303,6 +303,29 @@ ribo_status ribo_world_read_kernel_timing(ribo_world* w, ribo_kernel_timing* out
 // Number of kernels this library has launched in this process so far.
 uint64_t ribo_kernel_launch_count(void);
 
+// Allocation-free multigrid pressure solve.  No counterpart in the reference:
+// it exists for callers that cannot allocate device memory while they run
+// (a host that reserves its whole device budget at start-up and forbids
+// later allocations, or a frame loop that cannot absorb the synchronisation
+// cudaMalloc/cudaFree may cause).  It performs the world step's pressure
+// solve -- the same multigrid V-cycles, bit for bit -- on caller-owned
+// device buffers of fluid_w x fluid_h cells: divergence (f32), solid mask
+// (u32, 1 = wall) and pressure (f32, warm start in, result out).  The
+// multigrid hierarchy lives in a fixed ~6.2 MB array inside the library
+// that every GPU loading the library holds until the process exits; grids
+// above 512 x 512 cells are rejected with RIBO_INVALID_ARG.  It calls no
+// allocation routine.  The call is asynchronous on `cuda_stream` (0 = the
+// legacy default stream) on the calling thread's current device.  Its first
+// call on a device looks up the array's device address (once per device);
+// make that first call before any stream capture.  All calls share the one
+// array, so calls whose work overlaps on the GPU (other streams, other host
+// threads) race and must be serialised by the caller.  Zero multigrid
+// arguments take the reference values (8, 2, 2, 30, 1).
+ribo_status ribo_pressure_solve_noalloc(uint32_t fluid_w, uint32_t fluid_h, const float* d_divergence,
+                                        const uint32_t* d_solid_mask, float* d_pressure, uint32_t mg_min_size,
+                                        uint32_t mg_pre, uint32_t mg_post, uint32_t mg_coarse, uint32_t mg_cycles,
+                                        void* cuda_stream);
+
 #ifdef __cplusplus
 }  // extern "C"
 #endif
