@@ -203,8 +203,8 @@ __global__ void k_diffuse(const __grid_constant__ Dev d, const ribo_sim_params* 
 
 // fluid.wgsl:226-255
 __device__ __forceinline__ bool is_solid_at_pos(const Dev& d, float2 pos) {
-  int ix = rb_f2i(rb_floor(pos.x - 0.5f));
-  int iy = rb_f2i(rb_floor(pos.y - 0.5f));
+  int ix = rb_floor_i(pos.x - 0.5f);
+  int iy = rb_floor_i(pos.y - 0.5f);
   if (ix < 0 || ix >= d.fw || iy < 0 || iy >= d.fh) return true;
   return is_solid(d, ix, iy);
 }
@@ -212,7 +212,7 @@ __device__ __forceinline__ float2 sample_velocity(const Dev& d, const float2* vi
   float max_x = (float)d.fw - 0.5f, max_y = (float)d.fh - 0.5f;
   if (pos.x < 0.5f || pos.x > max_x || pos.y < 0.5f || pos.y > max_y) return f2(0.0f, 0.0f);
   float x = pos.x - 0.5f, y = pos.y - 0.5f;
-  int x0 = rb_f2i(rb_floor(x)), y0 = rb_f2i(rb_floor(y));
+  int x0 = rb_floor_i(x), y0 = rb_floor_i(y);
   float fx = rb_fract(x), fy = rb_fract(y);
   uint32_t cx0 = iclamp(x0, 0, d.fw - 1), cx1 = iclamp(x0 + 1, 0, d.fw - 1);
   uint32_t cy0 = iclamp(y0, 0, d.fh - 1), cy1 = iclamp(y0 + 1, 0, d.fh - 1);
@@ -252,6 +252,12 @@ __device__ __forceinline__ float curl_at(const Dev& d, const float2* vin, uint32
   float2 v_t = reflect_if_into_solid(d, x, yp, raw_velocity_cell(d, vin, x, yp));
   return 0.5f * (v_r.y - v_l.y) - 0.5f * (v_t.x - v_b.x);
 }
+// curl_at for every fluid cell (input of the confinement pass).
+__global__ void k_curl(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
+  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  d.curl[(size_t)y * d.fw + x] = curl_at(d, vin, x, y);
+}
 __global__ void k_vorticity(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
                             float2* __restrict__ vout) {
   uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
@@ -267,14 +273,16 @@ __global__ void k_vorticity(const __grid_constant__ Dev d, const ribo_sim_params
     vout[idx] = vin[idx];
     return;
   }
-  float w = curl_at(d, vin, x, y);
+  // curl_at of this cell and its 4 neighbours, precomputed once per cell by
+  // k_curl (the same function of the same inputs, so the same bits)
+  const float* cu = d.curl;
+  const int fw = d.fw;
+  float w = cu[idx];
   if (rb_abs(w) < (float)5e-4) {
     vout[idx] = vin[idx];
     return;
   }
-  float2 grad = mul2(f2(rb_abs(curl_at(d, vin, x + 1, y)) - rb_abs(curl_at(d, vin, x - 1, y)),
-                        rb_abs(curl_at(d, vin, x, y + 1)) - rb_abs(curl_at(d, vin, x, y - 1))),
-                     0.5f);
+  float2 grad = mul2(f2(rb_abs(cu[idx + 1]) - rb_abs(cu[idx - 1]), rb_abs(cu[idx + fw]) - rb_abs(cu[idx - fw])), 0.5f);
   float2 n = div2(grad, rb_max(len2(grad), (float)1e-5));
   float2 f = mul2(f2(n.y, -n.x), w * epsilon);
   float2 dv = clamp_len(mul2(f, fluid_dt(P)), 2.0f);
@@ -447,7 +455,8 @@ void launch_advect(const Dev& d, const ribo_sim_params* P, const float2* vin, fl
   RB_LAUNCH("advect_velocity", 17.0 * fc(d), s, k_advect<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
 }
 void launch_vorticity(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
-  RB_LAUNCH("vorticity", 17.0 * fc(d), s, k_vorticity<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+  RB_LAUNCH("curl", 12.0 * fc(d), s, k_curl<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin));
+  RB_LAUNCH("vorticity", 21.0 * fc(d), s, k_vorticity<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
 }
 void launch_divergence(const Dev& d, const float2* vin, cudaStream_t s) {
   RB_LAUNCH("divergence", 13.0 * fc(d), s, k_divergence<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin));

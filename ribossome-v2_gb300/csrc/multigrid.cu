@@ -513,7 +513,7 @@ static const char* const POST_NAMES[8] = {"mg_prolong_post_L0", "mg_prolong_post
 // the latency of one tile rather than by bandwidth.
 static bool small_tiles(const MgLevel& L) {
   const long big = (long)((L.nx + 63) / 64) * ((L.ny + 31) / 32);
-  return big < 2 * 152;
+  return big < 8 * 152;
 }
 
 template <int TW, int TH>

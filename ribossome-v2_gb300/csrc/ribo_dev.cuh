@@ -88,6 +88,7 @@ struct Dev {
   // fluid-resolution buffers
   uint8_t* mask;    // 1 = wall
   float2* normal;   // outward wall normal of each fluid cell (from the mask)
+  float* curl;      // curl of the velocity entering the confinement pass
   float2* va;     // velocity_a
   float2* vb;     // velocity_b
   float2* vsmooth;
@@ -225,7 +226,7 @@ __device__ __forceinline__ float2 raw_velocity_cell(const Dev& d, const float2* 
 // ---- light helpers used by the temperature pass (light.wgsl:46-102,182-189) ----
 __device__ __forceinline__ float light_above(const Dev& d, const ribo_sim_params* P, uint32_t x, uint32_t row, uint32_t band) {
   float sh = -P->sun_slope;
-  int base = rb_f2i(rb_floor(sh));
+  int base = rb_floor_i(sh);
   float f = sh - (float)base;
   float s = 0.0f;
   size_t bo = (size_t)band * d.lw * d.lh + (size_t)row * d.lw;

@@ -95,18 +95,38 @@ RB_HD float rb_smoothstep01(float x) {
 }
 
 // Saturating float -> integer conversions (WGSL semantics: NaN -> 0,
-// out-of-range values clamp to the nearest representable integer).
+// out-of-range values clamp to the nearest representable integer).  The
+// GPU's conversion instructions saturate and map NaN to 0 by definition,
+// so device code uses them directly; host code spells the same rule out.
 RB_HD int32_t rb_f2i(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rz(x);
+#else
   if (!(x == x)) return 0;
   if (x >= 2147483648.0f) return 2147483647;
   if (x <= -2147483648.0f) return (int32_t)0x80000000u;
   return (int32_t)x;
+#endif
 }
 
 RB_HD uint32_t rb_f2u(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2uint_rz(x);
+#else
   if (!(x > 0.0f)) return 0u;  // negatives, -0 and NaN
   if (x >= 4294967296.0f) return 0xffffffffu;
   return (uint32_t)x;
+#endif
+}
+
+// i32(floor(x)) with the saturating conversion above (one rounding-mode
+// conversion instruction on the GPU).
+RB_HD int32_t rb_floor_i(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rd(x);
+#else
+  return rb_f2i(rb_floor(x));
+#endif
 }
 
 // 2^k * p for k in [-252, 254] with at most one rounding.

@@ -59,6 +59,7 @@ struct World {
   // fluid resolution
   uint8_t* mask = nullptr;
   float2* normal = nullptr;
+  float* curl = nullptr;
   uint32_t* mask32 = nullptr;
   float2 *va = nullptr, *vb = nullptr, *vsmooth = nullptr;
   float *pa = nullptr, *pb = nullptr, *div = nullptr;

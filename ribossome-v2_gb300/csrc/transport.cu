@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ Dev d, 
   if (src_total > cap_self) p_diff = rb_min(CHEM_SQUEEZE_P * tn, 0.5f);
   float p_settle = 0.0f;
   if (g_src == 0u) p_settle = rb_min(MONOMER_SETTLE_P * rb_max(P->settle, 0.0f) * tn, 0.5f);
-  const int base_x = rb_f2i(rb_floor(disp.x)) - 1, base_y = rb_f2i(rb_floor(disp.y)) - 1;
+  const int base_x = rb_floor_i(disp.x) - 1, base_y = rb_floor_i(disp.y) - 1;
 
   float press[4] = {1.0f, 1.0f, 1.0f, 1.0f};
   float max_drop = 0.0f;
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ Dev d, 
       } else if (rfz < p_diff + p_settle) {
         py -= 1.0f;
       }
-      int offx = rb_f2i(rb_floor(px)) - base_x, offy = rb_f2i(rb_floor(py)) - base_y;
+      int offx = rb_floor_i(px) - base_x, offy = rb_floor_i(py) - base_y;
       uint32_t bi = (uint32_t)iclamp(offy, 0, 3) * 4u + (uint32_t)iclamp(offx, 0, 3);
       bins[bi] += unit;
     }
@@ -342,7 +342,7 @@ struct Smem {
 };
 }  // namespace st
 
-__global__ void __launch_bounds__(st::NT, 3) k_scatter_tiled(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
+__global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   st::Smem& S = *reinterpret_cast<st::Smem*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(st::NT, 3) k_scatter_tiled(const __grid_consta
         bound_start = f2(1.0f - rb_abs(2.0f * vx - 1.0f), 1.0f - rb_abs(2.0f * vy - 1.0f));
       }
       const bool disperse = g_src > 0u && (disp.x != 0.0f || disp.y != 0.0f);
-      const int basex = rb_f2i(rb_floor(disp.x)) - 1, basey = rb_f2i(rb_floor(disp.y)) - 1;
+      const int basex = rb_floor_i(disp.x) - 1, basey = rb_floor_i(disp.y) - 1;
       S.dispx[tid] = disp.x;
       S.dispy[tid] = disp.y;
       S.basex[tid] = basex;
@@ -665,7 +665,7 @@ __global__ void __launch_bounds__(st::NT, 3) k_scatter_tiled(const __grid_consta
       } else if (rfz < p_diff + p_settle) {
         py -= 1.0f;
       }
-      const int offx = rb_f2i(rb_floor(px)) - basex, offy = rb_f2i(rb_floor(py)) - basey;
+      const int offx = rb_floor_i(px) - basex, offy = rb_floor_i(py) - basey;
       const uint32_t bi = (uint32_t)iclamp(offy, 0, 3) * 4u + (uint32_t)iclamp(offx, 0, 3);
       const uint16_t sl = S.slot[bi][ct];
       if (sl != st::FAR) {

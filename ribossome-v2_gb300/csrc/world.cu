@@ -158,6 +158,7 @@ Dev World::dev() const {
   d.agg_nb = agg_nb;
   d.mask = mask;
   d.normal = normal;
+  d.curl = curl;
   d.va = va;
   d.vb = vb;
   d.vsmooth = vsmooth;
@@ -216,6 +217,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(agg_nb, C * 4);
   RB_ALLOC(mask, F);
   RB_ALLOC(normal, F * 8);
+  RB_ALLOC(curl, F * 4);
   RB_ALLOC(va, F * 8);
   RB_ALLOC(vb, F * 8);
   RB_ALLOC(vsmooth, F * 8);
