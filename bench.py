@@ -160,6 +160,17 @@ def max_over_ranks(ws, v):
     return float(t.item())
 
 
+def sum_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def cpu_sample(n, seconds_budget=15.0, max_steps=20):
     """The oracle (CPU restatement) on the host cores: a bounded sample of the workload."""
     import ribo_oracle
@@ -355,12 +366,123 @@ def run_ours(args):
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(n)
+    if not args.no_batched:
+        w.close()
+        bt = run_batched(args, local)
+        if ws > 1:  # replicas: every rank runs its own batch; whole-job throughput sums them
+            bt["batched"]["world_steps_per_s"] = sum_over_ranks(ws, bt["batched"]["world_steps_per_s"])
+            bt["plain"]["world_steps_per_s"] = sum_over_ranks(ws, bt["plain"]["world_steps_per_s"])
+        line["batched"] = bt
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def percentile(xs, q):
+    s = sorted(xs)
+    if not s:
+        return None
+    k = (len(s) - 1) * q / 100.0
+    lo = int(k)
+    hi = min(lo + 1, len(s) - 1)
+    return s[lo] + (s[hi] - s[lo]) * (k - lo)
+
+
+def run_batched(args, local):
+    """Batched worlds vs the plain per-world loop on the same GPU.
+
+    64 worlds of uneven sizes (synth.batch_specs: squares 128..1024 and the
+    rectangles 512x2048, 2048x256, fluid grid = env grid), the solver of the
+    full-size workload (4 V-cycles of 3+3 sweeps to 16x16, transport every
+    step).  Plain: one world after another through its own World API, each
+    stepped `steps` times.  Batched: all worlds as one ribo_batch, every pass
+    one launch over all of them, steps replayed from CUDA graphs.
+    Throughput = world-steps / device time; latency = device time of one
+    step as its caller sees it (one world's step alone, or one batched step
+    that advances every world).
+    """
+    import ribo_world as rw
+    import synth
+
+    specs = synth.batch_specs(args.batched_worlds)
+    worlds = []
+    total_cells = 0
+    for (gw, gh), seed, rock, mean in specs:
+        w = rw.World((gw, gh), seed=seed, mg_min_size=16, mg_pre=3, mg_post=3, device=local)
+        w.settings.fluid_substep = 1
+        w.settings.mg_cycles = 4
+        w.seed_inputs(synth.make_world_inputs((gw, gh), seed=seed, rock_frac=rock, monomer_mean=mean))
+        w.params = synth.bench_params(seed)
+        worlds.append(w)
+        total_cells += gw * gh
+    seeded = [w.ledger_blocking().total() for w in worlds]
+    steps = args.batched_steps
+    warm = max(args.warmup, 3)
+
+    # ---- plain per-world loop ----
+    for w in worlds:
+        w.run(warm)
+    for w in worlds:
+        w.sync()
+    plain_ms = 0.0
+    t = time.perf_counter()
+    for w in worlds:
+        w.mark(0)
+        w.run(steps)
+        w.mark(1)
+        plain_ms += w.elapsed_ms(0, 1)
+    plain_wall = time.perf_counter() - t
+    plain_lat = []
+    for w in worlds:
+        for _ in range(args.latency_samples):
+            w.mark(2)
+            w.encode_steps(1)
+            w.mark(3)
+            plain_lat.append(w.elapsed_ms(2, 3))
+
+    # ---- the same worlds as one batch ----
+    b = rw.Batch(worlds, device=local)
+    modes = b.autotune()
+    b.run(warm)
+    b.sync()
+    launches0 = rw.kernel_launch_count()
+    t = time.perf_counter()
+    b.mark(0)
+    b.run(steps)
+    b.mark(1)
+    batch_ms = b.elapsed_ms(0, 1)
+    batch_wall = time.perf_counter() - t
+    launches = rw.kernel_launch_count() - launches0
+    batch_lat = []
+    for _ in range(args.latency_samples * 4):
+        b.mark(2)
+        b.encode_steps(1)
+        b.mark(3)
+        batch_lat.append(b.elapsed_ms(2, 3))
+    b.sync()
+    b.close()
+    for w, s0 in zip(worlds, seeded):
+        if w.ledger_blocking().total() != s0:
+            raise RuntimeError("matter not conserved (batched)")
+    n = len(worlds)
+    plain = {"world_steps_per_s": n * steps / (plain_ms / 1000.0), "wall_world_steps_per_s": n * steps / plain_wall,
+             "step_latency_ms_p50": percentile(plain_lat, 50), "step_latency_ms_p99": percentile(plain_lat, 99)}
+    batched = {"world_steps_per_s": n * steps / (batch_ms / 1000.0), "wall_world_steps_per_s": n * steps / batch_wall,
+               "step_latency_ms_p50": percentile(batch_lat, 50), "step_latency_ms_p99": percentile(batch_lat, 99),
+               "gpu_launches": launches, "tile_modes": modes}
+    for w in worlds:
+        w.close()
+    return {
+        "workload": f"{n} worlds of uneven sizes (seeded draw from squares 128..1024 and 512x2048, 2048x256; "
+                    f"{total_cells / 1e6:.1f} M cells), 4 V-cycles 3+3 to 16x16, transport every step, "
+                    f"{steps} steps each",
+        "worlds": n, "steps": steps, "cells": total_cells, "plain": plain, "batched": batched,
+        "speedup": batched["world_steps_per_s"] / plain["world_steps_per_s"],
+        "latency_note": "plain: one world's step alone; batched: one batched step (advances every world)",
+    }
 
 
 def main():
@@ -374,6 +496,10 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-seconds", type=float, default=60.0)
+    ap.add_argument("--batched-worlds", type=int, default=64)
+    ap.add_argument("--batched-steps", type=int, default=200)
+    ap.add_argument("--latency-samples", type=int, default=5)
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

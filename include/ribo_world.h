@@ -303,6 +303,59 @@ ribo_status ribo_world_read_kernel_timing(ribo_world* w, ribo_kernel_timing* out
 // Number of kernels this library has launched in this process so far.
 uint64_t ribo_kernel_launch_count(void);
 
+// ---- Batches: many worlds advanced together ---------------------------------
+// No single counterpart in the reference, whose World::encode_steps
+// (src/world/mod.rs:1406-1632) advances one world per call; a batch runs that
+// same dispatch sequence for all of its member worlds in lock step.  Every
+// pass of a step is one launch over the tiles of all members (worlds of
+// different sizes and shapes); the multigrid V-cycle is one launch per level
+// index plus one coarse launch with a CTA per world; repeated step sequences
+// replay from one CUDA graph.  Each member's results are the same bits as
+// when it is stepped alone with the same parameters.  Members whose schedule
+// differs in a step (fluid substep parity, transport_every, settings) are
+// grouped and each group gets its own launches.  While a world is a member,
+// all of its work -- its own ribo_world_* calls included -- runs in order on
+// the batch's stream.  Members must live on the batch's device; a world
+// belongs to at most one batch.
+typedef struct ribo_batch ribo_batch;
+ribo_status ribo_batch_create(uint32_t device, ribo_batch** out);
+// Releases the members (it does not destroy them) and frees the batch.
+void ribo_batch_destroy(ribo_batch* b);
+ribo_status ribo_batch_add(ribo_batch* b, ribo_world* w);
+ribo_status ribo_batch_remove(ribo_batch* b, ribo_world* w);
+uint32_t ribo_batch_size(const ribo_batch* b);
+// Records `n` steps (1..64) of every member, asynchronously on the batch's
+// stream.  per_step[k * n + i] holds the parameters of step i of the k-th
+// member (membership order: the order of ribo_batch_add, less removals).
+ribo_status ribo_batch_step(ribo_batch* b, const ribo_sim_params* per_step, uint32_t n);
+// ribo_world_encode_steps for every member: params[k] is the k-th member's
+// SimParams; the per-step copies are derived from it with that member's
+// settings, and params[k].epoch advances by `n`.
+ribo_status ribo_batch_encode_steps(ribo_batch* b, ribo_sim_params* params, uint32_t n);
+// Ledgers after each step of the last ribo_batch_step / encode_steps call:
+// out[(k * n + i) * 12 + c] for member k, step i (members whose settings
+// have ledger_each_step; other members' entries are zero).  Waits.
+ribo_status ribo_batch_step_ledgers(ribo_batch* b, uint32_t* out, uint32_t n);
+// Waits for the batch's stream and checks every member's kernel status.
+ribo_status ribo_batch_sync(ribo_batch* b);
+// Timing marks on the batch's stream, as ribo_world_mark / elapsed_ms.
+ribo_status ribo_batch_mark(ribo_batch* b, uint32_t slot);
+ribo_status ribo_batch_elapsed_ms(ribo_batch* b, uint32_t slot_a, uint32_t slot_b, float* ms);
+// Tile-shape autotuner of the batched multigrid kernels: for every fine
+// level index it times the candidate tile shapes (by level size, 64x32
+// everywhere, 32x16 everywhere) on the members' current state with CUDA
+// events and keeps the fastest.  Tile shapes never change results (the
+// fused smoothers are bit-identical to one dispatch per half-sweep).
+// modes_out (optional, 8 entries) receives the choice per level index:
+// 0 = by level size, 1 = 64x32, 2 = 32x16.
+ribo_status ribo_batch_autotune(ribo_batch* b, uint32_t* modes_out);
+// Sets the tile shape per fine level index explicitly (modes as above; level
+// indices past n use 0).
+ribo_status ribo_batch_set_tile_modes(ribo_batch* b, const uint32_t* modes, uint32_t n);
+// Per-kernel timing of the next ribo_batch_step calls (as for a world).
+ribo_status ribo_batch_enable_kernel_timing(ribo_batch* b, int enable);
+ribo_status ribo_batch_read_kernel_timing(ribo_batch* b, ribo_kernel_timing* out, uint32_t cap, uint32_t* count);
+
 // Allocation-free multigrid pressure solve.  No counterpart in the reference:
 // it exists for callers that cannot allocate device memory while they run
 // (a host that reserves its whole device budget at start-up and forbids

@@ -8,13 +8,13 @@ namespace ribo {
 
 namespace {
 
-constexpr int BX = 32, BY = 8;
-
-inline dim3 grid2(int w, int h) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY); }
+constexpr int BX = PASS_BX, BY = PASS_BY;
 
 // fluid.wgsl:95-109,138-142,185-189
-__global__ void k_solid_mask(const __grid_constant__ Dev d) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_solid_mask(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   float gx = ((float)x + 0.5f) * d.sx, gy = ((float)y + 0.5f) * d.sy;
   float hx = d.sx * 0.25f, hy = d.sy * 0.25f;
@@ -35,8 +35,10 @@ __global__ void k_solid_mask(const __grid_constant__ Dev d) {
 }
 
 // fluid.wgsl:196-216, evaluated once per mask build for every fluid cell.
-__global__ void k_wall_normals(const __grid_constant__ Dev d) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_wall_normals(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   d.normal[(size_t)y * d.fw + x] = solid_normal(d, x, y);
 }
@@ -44,8 +46,10 @@ __global__ void k_wall_normals(const __grid_constant__ Dev d) {
 // fluid.wgsl:300-372 (update_temperature; copy_temperature becomes a
 // pointer swap on the host, and the redox_eaten reset happens here after
 // its single read).
-__global__ void k_temperature(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_temperature(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   const int fw = d.fw, fh = d.fh;
   size_t idx = (size_t)y * fw + x;
@@ -99,8 +103,10 @@ __device__ __forceinline__ uint32_t quant_force(float v) {
   int32_t q = rb_f2i(rb_rint(rb_clamp(v, (float)-1.0e5, (float)1.0e5) * FORCE_FP));
   return (uint32_t)q;
 }
-__global__ void k_forces(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_forces(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
   uint2 fv = reinterpret_cast<uint2*>(d.force_vec)[idx];
@@ -147,9 +153,12 @@ __device__ __forceinline__ float2 slope_steer(const Dev& d, const ribo_sim_param
 
 // fluid.wgsl:410-432 (add_forces; clear_forces is dropped: gather
 // overwrites every fluid_forces entry before the next read)
-__global__ void k_add_forces(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
-                             float2* __restrict__ vout) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_add_forces(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  float2* __restrict__ vout = dir ? d.va : d.vb;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   const int fw = d.fw;
   size_t idx = (size_t)y * fw + x;
@@ -174,9 +183,12 @@ __global__ void k_add_forces(const __grid_constant__ Dev d, const ribo_sim_param
 }
 
 // fluid.wgsl:435-456
-__global__ void k_diffuse(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
-                          float2* __restrict__ vout) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_diffuse(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  float2* __restrict__ vout = dir ? d.va : d.vb;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
   if (is_solid(d, x, y)) {
@@ -221,9 +233,12 @@ __device__ __forceinline__ float2 sample_velocity(const Dev& d, const float2* vi
   return mix2(v0, v1, fy);
 }
 // fluid.wgsl:458-477
-__global__ void k_advect(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
-                         float2* __restrict__ vout) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_advect(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  float2* __restrict__ vout = dir ? d.va : d.vb;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
   if (is_solid(d, x, y)) {
@@ -253,14 +268,20 @@ __device__ __forceinline__ float curl_at(const Dev& d, const float2* vin, uint32
   return 0.5f * (v_r.y - v_l.y) - 0.5f * (v_t.x - v_b.x);
 }
 // curl_at for every fluid cell (input of the confinement pass).
-__global__ void k_curl(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_curl(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   d.curl[(size_t)y * d.fw + x] = curl_at(d, vin, x, y);
 }
-__global__ void k_vorticity(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P, const float2* __restrict__ vin,
-                            float2* __restrict__ vout) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_vorticity(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  float2* __restrict__ vout = dir ? d.va : d.vb;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
   if (is_solid(d, x, y)) {
@@ -297,8 +318,11 @@ __device__ __forceinline__ float2 div_neighbor(const Dev& d, const float2* vin, 
   if (outside || is_solid(d, nx, ny)) return axis_x ? f2(-v_c.x, v_c.y) : f2(v_c.x, -v_c.y);
   return raw_velocity_cell(d, vin, nx, ny);
 }
-__global__ void k_divergence(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
-  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_divergence(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  int x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= d.fw || y >= d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
   if (is_solid(d, x, y)) {
@@ -314,8 +338,12 @@ __global__ void k_divergence(const __grid_constant__ Dev d, const float2* __rest
 }
 
 // fluid.wgsl:610-630
-__global__ void k_subtract_gradient(const __grid_constant__ Dev d, const float2* __restrict__ vin, float2* __restrict__ vout) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_subtract_gradient(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  float2* __restrict__ vout = dir ? d.va : d.vb;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   const int fw = d.fw;
   size_t idx = (size_t)y * fw + x;
@@ -343,13 +371,16 @@ __global__ void k_subtract_gradient(const __grid_constant__ Dev d, const float2*
 // tile with coalesced loads, while warp 0 (lane = line) runs the 32 serial
 // add chains over the previous chunk.  Row blocks and column blocks share
 // one launch.
-constexpr int NF_L = 32, NF_C = 128, NF_THREADS = 256;
-__global__ void __launch_bounds__(NF_THREADS) k_net_flux(const __grid_constant__ Dev d, const float2* __restrict__ vin,
-                                                         int row_blocks) {
+constexpr int NF_L = NET_FLUX_LINES, NF_C = 128, NF_THREADS = 256;
+template <class S>
+__global__ void __launch_bounds__(NF_THREADS) k_net_flux(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  const int row_blocks = (d.fh + NF_L - 1) / NF_L;
   __shared__ float val[2][NF_L][NF_C + 1];
   __shared__ uint8_t wall[2][NF_L][NF_C + 4];
-  const bool rows = (int)blockIdx.x < row_blocks;
-  const int line0 = (rows ? (int)blockIdx.x : (int)blockIdx.x - row_blocks) * NF_L;
+  const bool rows = (int)cta.bx < row_blocks;
+  const int line0 = (rows ? (int)cta.bx : (int)cta.bx - row_blocks) * NF_L;
   const int nlines = rows ? d.fh : d.fw;
   const int len = rows ? d.fw : d.fh;
   const int nchunks = (len + NF_C - 1) / NF_C;
@@ -400,8 +431,12 @@ __global__ void __launch_bounds__(NF_THREADS) k_net_flux(const __grid_constant__
 }
 
 // fluid.wgsl:663-677
-__global__ void k_boundaries(const __grid_constant__ Dev d, const float2* __restrict__ vin, float2* __restrict__ vout) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_boundaries(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  float2* __restrict__ vout = dir ? d.va : d.vb;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
   if (is_solid(d, x, y)) {
@@ -417,8 +452,11 @@ __global__ void k_boundaries(const __grid_constant__ Dev d, const float2* __rest
 }
 
 // fluid.wgsl:680-693
-__global__ void k_smooth(const __grid_constant__ Dev d, const float2* __restrict__ vin) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_smooth(const __grid_constant__ S s, int dir) {
+  RB_WORLD(s);
+  const float2* __restrict__ vin = dir ? d.vb : d.va;
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   const int fw = d.fw;
   uint32_t xm = x > 0u ? x - 1u : x, xp = umin(x + 1u, (uint32_t)fw - 1u);
@@ -432,47 +470,44 @@ __global__ void k_smooth(const __grid_constant__ Dev d, const float2* __restrict
 
 }  // namespace
 
-inline double fc(const Dev& d) { return (double)d.fw * d.fh; }
-inline double gc(const Dev& d) { return (double)d.gw * d.gh; }
-
-void launch_solid_mask(const Dev& d, cudaStream_t s) {
-  RB_LAUNCH("build_solid_mask", 4.0 * gc(d) + fc(d), s, k_solid_mask<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d));
-  RB_LAUNCH("wall_normals", 9.0 * fc(d), s, k_wall_normals<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d));
+void launch_solid_mask(const Target& t, cudaStream_t s) {
+  const dim3 blk(BX, BY);
+  RB_PASS("build_solid_mask", 4.0 * t.cells + t.fcells, s, t, GEO_FLUID, blk, 0, k_solid_mask, nullptr);
+  RB_PASS("wall_normals", 9.0 * t.fcells, s, t, GEO_FLUID, blk, 0, k_wall_normals, nullptr);
 }
-void launch_temperature(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
-  RB_LAUNCH("update_temperature", 41.0 * fc(d) + 4.0 * gc(d), s, k_temperature<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P));
+void launch_temperature(const Target& t, cudaStream_t s) {
+  RB_PASS("update_temperature", 41.0 * t.fcells + 4.0 * t.cells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_temperature, nullptr);
 }
-void launch_forces(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
-  RB_LAUNCH("forces", 28.0 * fc(d), s, k_forces<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P));
+void launch_forces(const Target& t, cudaStream_t s) {
+  RB_PASS("forces", 28.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_forces, nullptr);
 }
-void launch_add_forces(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
-  RB_LAUNCH("add_forces", 33.0 * fc(d) + 4.0 * gc(d), s, k_add_forces<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+void launch_add_forces(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("add_forces", 33.0 * t.fcells + 4.0 * t.cells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_add_forces, nullptr, dir);
 }
-void launch_diffuse(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
-  RB_LAUNCH("diffuse_velocity", 17.0 * fc(d), s, k_diffuse<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+void launch_diffuse(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("diffuse_velocity", 17.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_diffuse, nullptr, dir);
 }
-void launch_advect(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
-  RB_LAUNCH("advect_velocity", 17.0 * fc(d), s, k_advect<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+void launch_advect(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("advect_velocity", 17.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_advect, nullptr, dir);
 }
-void launch_vorticity(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s) {
-  RB_LAUNCH("curl", 12.0 * fc(d), s, k_curl<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin));
-  RB_LAUNCH("vorticity", 21.0 * fc(d), s, k_vorticity<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, P, vin, vout));
+void launch_vorticity(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("curl", 12.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_curl, nullptr, dir);
+  RB_PASS("vorticity", 21.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_vorticity, nullptr, dir);
 }
-void launch_divergence(const Dev& d, const float2* vin, cudaStream_t s) {
-  RB_LAUNCH("divergence", 13.0 * fc(d), s, k_divergence<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin));
+void launch_divergence(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("divergence", 13.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_divergence, nullptr, dir);
 }
-void launch_subtract_gradient(const Dev& d, const float2* vin, float2* vout, cudaStream_t s) {
-  RB_LAUNCH("subtract_gradient", 21.0 * fc(d), s, k_subtract_gradient<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin, vout));
+void launch_subtract_gradient(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("subtract_gradient", 21.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_subtract_gradient, nullptr, dir);
 }
-void launch_net_flux(const Dev& d, const float2* vin, cudaStream_t s) {
-  int row_blocks = (d.fh + NF_L - 1) / NF_L, col_blocks = (d.fw + NF_L - 1) / NF_L;
-  RB_LAUNCH("net_flux", 18.0 * fc(d), s, k_net_flux<<<row_blocks + col_blocks, NF_THREADS, 0, s>>>(d, vin, row_blocks));
+void launch_net_flux(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("net_flux", 18.0 * t.fcells, s, t, GEO_NET_FLUX, dim3(NF_THREADS), 0, k_net_flux, nullptr, dir);
 }
-void launch_boundaries(const Dev& d, const float2* vin, float2* vout, cudaStream_t s) {
-  RB_LAUNCH("enforce_boundaries", 17.0 * fc(d), s, k_boundaries<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin, vout));
+void launch_boundaries(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("enforce_boundaries", 17.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_boundaries, nullptr, dir);
 }
-void launch_smooth(const Dev& d, const float2* vin, cudaStream_t s) {
-  RB_LAUNCH("smooth_velocity", 16.0 * fc(d), s, k_smooth<<<grid2(d.fw, d.fh), dim3(BX, BY), 0, s>>>(d, vin));
+void launch_smooth(const Target& t, int dir, cudaStream_t s) {
+  RB_PASS("smooth_velocity", 16.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_smooth, nullptr, dir);
 }
 
 }  // namespace ribo

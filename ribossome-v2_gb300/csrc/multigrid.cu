@@ -6,6 +6,10 @@
 // Red-black sweeps update one colour from the other colour only, so every
 // fused or tiled variant below produces the same bits as one dispatch per
 // half-sweep.
+#include <string.h>
+
+#include <vector>
+
 #include "ribo_dev.cuh"
 #include "ribo_launch.h"
 #include "ribo_tma.cuh"
@@ -159,6 +163,51 @@ struct BoxMaps {
   CUtensorMap p, rhs, fl;
 };
 
+// One fine level of one world in a fused pre- or post-smooth launch.
+struct MgPass {
+  Lv L, C;               // the level and the next coarser one
+  const float* p_src;    // p loaded with the box (pre on level 0: pressure_a; post: pre-smoothed p)
+  const float* r_src;    // right-hand side of the level
+  const uint8_t* f_src;  // water flags of the level
+  float* p_out;          // smoothed p of the level
+  uint32_t* status;      // the world's kernel status word
+};
+// A launch over one world's level (tensor maps in parameter space when the
+// kernel loads with TMA), or over the same level index of a batch of worlds
+// (plain loads; the CTA finds its world as the per-cell passes do).
+struct MgOne {
+  MgPass e;
+  BoxMaps maps;
+};
+struct MgSet {
+  const MgPass* e;
+  const int* start;  // [n + 1]
+  const int* nbx;    // [n]
+  int n;
+};
+__device__ __forceinline__ const BoxMaps* mg_locate(const MgOne& s, MgPass& e, int& tx, int& ty) {
+  e = s.e;
+  tx = (int)blockIdx.x;
+  ty = (int)blockIdx.y;
+  return &s.maps;
+}
+__device__ __forceinline__ const BoxMaps* mg_locate(const MgSet& s, MgPass& e, int& tx, int& ty) {
+  const int w = batch_member(s.start, s.n);
+  e = s.e[w];
+  const int r = (int)blockIdx.x - __ldg(s.start + w), nb = __ldg(s.nbx + w);
+  tx = r % nb;
+  ty = r / nb;
+  return nullptr;
+}
+template <class S>
+struct MgHasMaps {
+  static constexpr bool value = false;
+};
+template <>
+struct MgHasMaps<MgOne> {
+  static constexpr bool value = true;
+};
+
 // The neighbour sum of multigrid.wgsl:34-45 in branch-free form: adding the
 // +0.0 of a non-water neighbour leaves the running sum unchanged (it starts
 // at +0.0 and can never become -0.0 in round-to-nearest).
@@ -179,9 +228,9 @@ __device__ __forceinline__ float gs_update(const float* sp, const float* sr, con
 }
 
 template <int TW, int TH, bool TMA, bool TOP, bool LOADP>
-__device__ __forceinline__ bool box_load(const Dev& d, const Lv& L, const float* __restrict__ p_src,
+__device__ __forceinline__ bool box_load(uint32_t* status, const Lv& L, const float* __restrict__ p_src,
                                          const float* __restrict__ r_src, const uint8_t* __restrict__ f_src,
-                                         const BoxMaps& maps, int bx, int by, int RH, float* sp, float* sr, uint8_t* sf,
+                                         const BoxMaps* maps, int bx, int by, int RH, float* sp, float* sr, uint8_t* sf,
                                          uint64_t* bar) {
   constexpr int BOXW = TW + 2 * BOXX;
   const int n = BOXW * RH;
@@ -190,14 +239,14 @@ __device__ __forceinline__ bool box_load(const Dev& d, const Lv& L, const float*
     if (tid == 0) {
       mbar_init(bar, 1);
       mbar_expect_tx(bar, (uint32_t)((LOADP ? 4 : 0) * n + 4 * n + n));
-      if (LOADP) tma_load_2d(sp, &maps.p, bx, by, bar);
-      tma_load_2d(sr, &maps.rhs, bx, by, bar);
-      tma_load_2d(sf, &maps.fl, bx, by, bar);
+      if (LOADP) tma_load_2d(sp, &maps->p, bx, by, bar);
+      tma_load_2d(sr, &maps->rhs, bx, by, bar);
+      tma_load_2d(sf, &maps->fl, bx, by, bar);
     }
     if (!LOADP)
       for (int e = tid; e < n; e += BX * BY) sp[e] = 0.0f;
     __syncthreads();
-    if (!mbar_wait_bounded(bar, 0, d.status)) return false;
+    if (!mbar_wait_bounded(bar, 0, status)) return false;
   } else {
     for (int e = tid; e < n; e += BX * BY) {
       int gx = bx + e % BOXW, gy = by + e / BOXW;
@@ -256,11 +305,15 @@ __device__ __forceinline__ void box_store(const Lv& L, float* __restrict__ p_out
 }
 
 // Pre-smooth (nu sweeps) + residual + restrict (multigrid.wgsl:60-105).
-template <int TW, int TH, bool TMA, bool TOP>
-__global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ Dev d, Lv L, Lv C,
-                                                   const __grid_constant__ BoxMaps maps, const float* __restrict__ p_src,
-                                                   const float* __restrict__ r_src, const uint8_t* __restrict__ f_src,
-                                                   float* __restrict__ p_out, int nu) {
+template <int TW, int TH, bool TMA, bool TOP, class S>
+__global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ S s, int nu) {
+  static_assert(!TMA || MgHasMaps<S>::value, "TMA loads need the tensor maps of a one-world launch");
+  MgPass e;
+  int tile_x, tile_y;
+  const BoxMaps* maps = mg_locate(s, e, tile_x, tile_y);
+  const Lv& L = e.L;
+  const Lv& C = e.C;
+  float* __restrict__ p_out = e.p_out;
   constexpr int BOXW = TW + 2 * BOXX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -268,15 +321,15 @@ __global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ Dev d
   float* sp = reinterpret_cast<float*>(smem_raw);
   float* sr = sp + BOXW * RH;
   uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
-  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+  const int x0 = tile_x * TW, y0 = tile_y * TH;
   const int bx = x0 - BOXX, by = y0 - H;
-  if (!box_load<TW, TH, TMA, TOP, TOP>(d, L, p_src, r_src, f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
+  if (!box_load<TW, TH, TMA, TOP, TOP>(e.status, L, e.p_src, e.r_src, e.f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
   box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, L.eps, sp, sr, sf);
   box_store<TW, TH>(L, p_out, x0, y0, H, sp);
   // residual of the 4 children of each coarse cell of the tile, x2 average
   for (int cj = threadIdx.y; cj < TH / 2; cj += BY)
     for (int ci = threadIdx.x; ci < TW / 2; ci += BX) {
-      int cgx = blockIdx.x * (TW / 2) + ci, cgy = blockIdx.y * (TH / 2) + cj;
+      int cgx = tile_x * (TW / 2) + ci, cgy = tile_y * (TH / 2) + cj;
       if (cgx >= C.nx || cgy >= C.ny) continue;
       float sum = 0.0f;
       uint32_t nf = 0;
@@ -301,11 +354,15 @@ __global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ Dev d
 
 // Prolong (add the coarse correction to water cells) + post-smooth nu sweeps
 // (multigrid.wgsl:108-114, 60-77).
-template <int TW, int TH, bool TMA>
-__global__ void __launch_bounds__(BX* BY) k_mg_post(const __grid_constant__ Dev d, Lv L, Lv C,
-                                                    const __grid_constant__ BoxMaps maps, const float* __restrict__ p_src,
-                                                    const float* __restrict__ r_src, const uint8_t* __restrict__ f_src,
-                                                    float* __restrict__ p_out, int nu) {
+template <int TW, int TH, bool TMA, class S>
+__global__ void __launch_bounds__(BX* BY) k_mg_post(const __grid_constant__ S s, int nu) {
+  static_assert(!TMA || MgHasMaps<S>::value, "TMA loads need the tensor maps of a one-world launch");
+  MgPass e;
+  int tile_x, tile_y;
+  const BoxMaps* maps = mg_locate(s, e, tile_x, tile_y);
+  const Lv& L = e.L;
+  const Lv& C = e.C;
+  float* __restrict__ p_out = e.p_out;
   constexpr int BOXW = TW + 2 * BOXX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -313,9 +370,9 @@ __global__ void __launch_bounds__(BX* BY) k_mg_post(const __grid_constant__ Dev 
   float* sp = reinterpret_cast<float*>(smem_raw);
   float* sr = sp + BOXW * RH;
   uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
-  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+  const int x0 = tile_x * TW, y0 = tile_y * TH;
   const int bx = x0 - BOXX, by = y0 - H;
-  if (!box_load<TW, TH, TMA, false, true>(d, L, p_src, r_src, f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
+  if (!box_load<TW, TH, TMA, false, true>(e.status, L, e.p_src, e.r_src, e.f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
   const int n = BOXW * RH;
   for (int e = threadIdx.y * BX + threadIdx.x; e < n; e += BX * BY) {
     if (!sf[e]) continue;
@@ -337,6 +394,26 @@ struct CoarseSet {
   const uint8_t* fl_top;
   float* p_out;  // level `top` result
 };
+// The coarse V-cycle of one world: its levels from the first one that fits
+// in shared memory down, and, when that is level 0 (top), the world's own
+// pressure_a, divergence and wall mask.
+struct CoarsePass {
+  CoarseSet cs;
+  const uint8_t* mask;
+  const float* div;
+  float* pa;
+  int fw;
+  int top;
+};
+struct CoarseOne {
+  CoarsePass e;
+};
+struct CoarseMany {
+  const CoarsePass* e;  // [n], one CTA each
+  int n;
+};
+__device__ __forceinline__ const CoarsePass& coarse_of(const CoarseOne& s) { return s.e; }
+__device__ __forceinline__ const CoarsePass& coarse_of(const CoarseMany& s) { return s.e[blockIdx.x]; }
 
 // One colour of a red-black sweep on a level held in shared memory: the
 // block is viewed as 32 x (COARSE_THREADS/32) threads walking the cells of
@@ -358,9 +435,11 @@ __device__ __forceinline__ void sm_sweep(int nx, int ny, float eps, float* p, co
   __syncthreads();
 }
 
-template <bool TOP>
-__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ Dev d, const __grid_constant__ CoarseSet cs,
-                                                              int nu_pre, int nu_post, int coarse) {
+template <class S>
+__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ S s, int nu_pre, int nu_post, int coarse) {
+  const CoarsePass& e = coarse_of(s);
+  const CoarseSet& cs = e.cs;
+  const bool TOP = e.top != 0;
   extern __shared__ float smem[];
   int total = cs.off[cs.n - 1] + cs.nx[cs.n - 1] * cs.ny[cs.n - 1];
   float* P = smem;
@@ -373,10 +452,10 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
       float r, p = 0.0f;
       if (TOP) {
         int y = idx / cs.nx[0], x = idx - y * cs.nx[0];
-        size_t gi = (size_t)y * d.fw + x;
-        f = d.mask[gi] ? 0 : 1;
-        r = d.div[gi];
-        p = f ? d.pa[gi] : 0.0f;
+        size_t gi = (size_t)y * e.fw + x;
+        f = e.mask[gi] ? 0 : 1;
+        r = e.div[gi];
+        p = f ? e.pa[gi] : 0.0f;
       } else {
         f = cs.fl_top[idx];
         r = cs.rhs_top[idx];
@@ -453,7 +532,7 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
       if (TOP) {
         int y = idx / cs.nx[0], x = idx - y * cs.nx[0];
-        d.pa[(size_t)y * d.fw + x] = P[idx];
+        e.pa[(size_t)y * e.fw + x] = P[idx];
       } else {
         cs.p_out[idx] = P[idx];
       }
@@ -561,12 +640,15 @@ bool multigrid_make_maps(const MgLevel* levels, int nl, const MgConfig& c, const
 
 template <int TW, int TH>
 static void set_tile_attrs(int mx) {
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_post<TW, TH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_post<TW, TH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, true, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, false, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, true, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, false, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, true, MgSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, false, MgSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_post<TW, TH, true, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_post<TW, TH, false, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_post<TW, TH, false, MgSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
 static void set_smem_attrs() {
@@ -577,54 +659,37 @@ static void set_smem_attrs() {
   const int mx = 200 * 1024;
   set_tile_attrs<64, 32>(mx);
   set_tile_attrs<32, 16>(mx);
-  cudaFuncSetAttribute(k_mg_coarse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_coarse<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_coarse<CoarseOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_coarse<CoarseMany>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   attr_done |= 1ull << (dev & 63);
 }
 
-template <int TW, int TH>
-static void launch_pre(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
+// The pre- and post-smooth passes of fine level l.  Level 0 reads
+// pressure_a (masked) and the divergence directly and its post pass writes
+// pressure_a; the pre-smoothed p goes to p_tmp (level 0) or p2.
+static MgPass pre_pass(const Dev& d, const MgLevel* levels, int l, const MgBufs& b) {
   const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
-  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
-  const size_t sm = box_smem<TW, TH>(2 * c.pre + 1);
-  const bool tma = b.maps && b.maps[l].ok;
-  const BoxMaps maps = tma ? BoxMaps{b.maps[l].pre_p, b.maps[l].pre_rhs, b.maps[l].pre_fl} : BoxMaps{};
-  const float* rhs = l == 0 ? d.div : L.rhs;
-  float* pout = l == 0 ? b.p_tmp : b.p2 + levels[l].off;
-  const char* name = PRE_NAMES[l < 7 ? l : 7];
-  const double bytes = (l == 0 ? 13.0 : 9.0) * cells(L) + 5.0 * cells(C);
-  if (tma && l == 0)
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, true><<<grid, blk, sm, s>>>(d, L, C, maps, d.pa, rhs, L.fl, pout, c.pre));
-  else if (tma)
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, false><<<grid, blk, sm, s>>>(d, L, C, maps, nullptr, rhs, L.fl, pout, c.pre));
-  else if (l == 0)
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, true><<<grid, blk, sm, s>>>(d, L, C, maps, d.pa, rhs, L.fl, pout, c.pre));
-  else
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, false><<<grid, blk, sm, s>>>(d, L, C, maps, nullptr, rhs, L.fl, pout, c.pre));
+  return MgPass{L, C, l == 0 ? d.pa : nullptr, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? b.p_tmp : b.p2 + levels[l].off,
+                d.status};
+}
+static MgPass post_pass(const Dev& d, const MgLevel* levels, int l, const MgBufs& b) {
+  const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
+  return MgPass{L, C, l == 0 ? b.p_tmp : b.p2 + levels[l].off, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? d.pa : L.p,
+                d.status};
+}
+static double pre_bytes(const MgLevel* levels, int l) {
+  return (l == 0 ? 13.0 : 9.0) * (double)levels[l].nx * levels[l].ny + 5.0 * (double)levels[l + 1].nx * levels[l + 1].ny;
+}
+static double post_bytes(const MgLevel* levels, int l) {
+  return 13.0 * (double)levels[l].nx * levels[l].ny + 4.0 * (double)levels[l + 1].nx * levels[l + 1].ny;
 }
 
-template <int TW, int TH>
-static void launch_post(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
-  const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
-  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
-  const size_t sm = box_smem<TW, TH>(2 * c.post);
-  const bool tma = b.maps && b.maps[l].ok;
-  const BoxMaps maps = tma ? BoxMaps{b.maps[l].post_p, b.maps[l].post_rhs, b.maps[l].post_fl} : BoxMaps{};
-  const float* rhs = l == 0 ? d.div : L.rhs;
-  const float* pin = l == 0 ? b.p_tmp : b.p2 + levels[l].off;
-  float* pout = l == 0 ? d.pa : L.p;
-  const double bytes = 13.0 * cells(L) + 4.0 * cells(C);
-  const char* name = POST_NAMES[l < 7 ? l : 7];
-  if (tma)
-    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, true><<<grid, blk, sm, s>>>(d, L, C, maps, pin, rhs, L.fl, pout, c.post));
-  else
-    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, false><<<grid, blk, sm, s>>>(d, L, C, maps, pin, rhs, L.fl, pout, c.post));
-}
-
-void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
-  set_smem_attrs();
+// The coarse V-cycle of one world (levels from the first one that fits in
+// shared memory down) and its shared-memory size.
+static CoarsePass coarse_pass(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, size_t* smem, double* bytes) {
   const int k = multigrid_first_coarse_level(levels, nl);
-  CoarseSet cs{};
+  CoarsePass e{};
+  CoarseSet& cs = e.cs;
   cs.n = nl - k;
   int off = 0;
   for (int l = k; l < nl; l++) {
@@ -637,25 +702,247 @@ void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const M
   cs.rhs_top = b.rhs + levels[k].off;
   cs.fl_top = b.fluid + levels[k].off;
   cs.p_out = b.p + levels[k].off;
-  const size_t coarse_smem = (size_t)off * 9 + 16;
-  const double coarse_bytes = 13.0 * levels[k].nx * levels[k].ny;
+  e.mask = d.mask;
+  e.div = d.div;
+  e.pa = d.pa;
+  e.fw = d.fw;
+  e.top = k == 0 ? 1 : 0;
+  *smem = (size_t)off * 9 + 16;
+  *bytes = 13.0 * levels[k].nx * levels[k].ny;
+  return e;
+}
+
+template <int TW, int TH>
+static void launch_pre(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
+  MgOne one{pre_pass(d, levels, l, b), BoxMaps{}};
+  const Lv& L = one.e.L;
+  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
+  const size_t sm = box_smem<TW, TH>(2 * c.pre + 1);
+  const bool tma = b.maps && b.maps[l].ok;
+  if (tma) one.maps = BoxMaps{b.maps[l].pre_p, b.maps[l].pre_rhs, b.maps[l].pre_fl};
+  const char* name = PRE_NAMES[l < 7 ? l : 7];
+  const double bytes = pre_bytes(levels, l);
+  if (tma && l == 0)
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, true, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
+  else if (tma)
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, false, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
+  else if (l == 0)
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, true, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
+  else
+    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, false, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
+}
+
+template <int TW, int TH>
+static void launch_post(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
+  MgOne one{post_pass(d, levels, l, b), BoxMaps{}};
+  const Lv& L = one.e.L;
+  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
+  const size_t sm = box_smem<TW, TH>(2 * c.post);
+  const bool tma = b.maps && b.maps[l].ok;
+  if (tma) one.maps = BoxMaps{b.maps[l].post_p, b.maps[l].post_rhs, b.maps[l].post_fl};
+  const double bytes = post_bytes(levels, l);
+  const char* name = POST_NAMES[l < 7 ? l : 7];
+  if (tma)
+    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, true, MgOne><<<grid, blk, sm, s>>>(one, c.post));
+  else
+    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, false, MgOne><<<grid, blk, sm, s>>>(one, c.post));
+}
+
+void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
+  set_smem_attrs();
+  const int k = multigrid_first_coarse_level(levels, nl);
+  size_t coarse_smem = 0;
+  double coarse_bytes = 0.0;
+  const CoarseOne co{coarse_pass(d, levels, nl, b, &coarse_smem, &coarse_bytes)};
   const int cycles = c.cycles < 1 ? 1 : c.cycles;
   for (int cy = 0; cy < cycles; cy++) {
     for (int l = 0; l < k; l++) {
       if (small_tiles(levels[l])) launch_pre<32, 16>(d, levels, l, b, c, s);
       else launch_pre<64, 32>(d, levels, l, b, c, s);
     }
-    if (k == 0)
-      RB_LAUNCH("mg_coarse_vcycle", coarse_bytes, s,
-                k_mg_coarse<true><<<1, COARSE_THREADS, coarse_smem, s>>>(d, cs, c.pre, c.post, c.coarse));
-    else
-      RB_LAUNCH("mg_coarse_vcycle", coarse_bytes, s,
-                k_mg_coarse<false><<<1, COARSE_THREADS, coarse_smem, s>>>(d, cs, c.pre, c.post, c.coarse));
+    RB_LAUNCH("mg_coarse_vcycle", coarse_bytes, s,
+              k_mg_coarse<CoarseOne><<<1, COARSE_THREADS, coarse_smem, s>>>(co, c.pre, c.post, c.coarse));
     for (int l = k - 1; l >= 0; l--) {
       if (small_tiles(levels[l])) launch_post<32, 16>(d, levels, l, b, c, s);
       else launch_post<64, 32>(d, levels, l, b, c, s);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Batched V-cycles.  Worlds of different sizes have different numbers of
+// fine levels; every launch covers one fine level index (and one tile
+// shape) of the worlds that have it, in V order: pre-smooth level 0, 1, ...,
+// the coarse solves (one CTA per world), post-smooth ..., 1, 0.  Each world
+// sees its own kernels in its own order, so its results are the same bits
+// as when it is stepped alone.
+
+struct MgBatchPlan {
+  struct Group {
+    int level;   // fine level index
+    bool small;  // 32x16 tiles (else 64x32)
+    int n, total;
+    const MgPass* pre;  // device [n]
+    const MgPass* post;
+    const int* start;  // device [n + 1]
+    const int* nbx;    // device [n]
+    double bytes_pre, bytes_post;
+  };
+  MgConfig c{};
+  std::vector<Group> groups;
+  int levels = 0;
+  int n = 0;
+  const CoarsePass* coarse = nullptr;
+  size_t coarse_smem = 0;
+  double coarse_bytes = 0.0;
+  void* blob = nullptr;
+};
+
+MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, const int* tile_mode, int nmodes,
+                                  cudaStream_t s) {
+  MgBatchPlan* plan = new MgBatchPlan;
+  plan->c = c;
+  plan->n = n;
+  std::vector<unsigned char> host;
+  auto put = [&](const void* p, size_t bytes) {
+    size_t off = (host.size() + 63) & ~(size_t)63;
+    host.resize(off + bytes);
+    if (bytes) memcpy(host.data() + off, p, bytes);
+    return off;
+  };
+  struct Offs {
+    size_t pre, post, start, nbx;
+  };
+  std::vector<Offs> offs;
+  for (int w = 0; w < n; w++) {
+    int k = multigrid_first_coarse_level(ws[w].levels, ws[w].nlevels);
+    if (k > plan->levels) plan->levels = k;
+  }
+  for (int l = 0; l < plan->levels; l++) {
+    for (int small = 0; small < 2; small++) {
+      std::vector<MgPass> pre, post;
+      std::vector<int> start(1, 0), nbx;
+      double bpre = 0.0, bpost = 0.0;
+      for (int w = 0; w < n; w++) {
+        const MgWorld& W = ws[w];
+        if (l >= multigrid_first_coarse_level(W.levels, W.nlevels)) continue;
+        const int mode = l < nmodes ? tile_mode[l] : 0;
+        const bool sm = mode == 1 ? false : (mode == 2 ? true : small_tiles(W.levels[l]));
+        if (sm != (small != 0)) continue;
+        const int tw = sm ? 32 : 64, th = sm ? 16 : 32;
+        const int bx = (W.levels[l].nx + tw - 1) / tw, by = (W.levels[l].ny + th - 1) / th;
+        pre.push_back(pre_pass(W.d, W.levels, l, W.b));
+        post.push_back(post_pass(W.d, W.levels, l, W.b));
+        nbx.push_back(bx);
+        start.push_back(start.back() + bx * by);
+        bpre += pre_bytes(W.levels, l);
+        bpost += post_bytes(W.levels, l);
+      }
+      if (pre.empty()) continue;
+      MgBatchPlan::Group g{};
+      g.level = l;
+      g.small = small != 0;
+      g.n = (int)pre.size();
+      g.total = start.back();
+      g.bytes_pre = bpre;
+      g.bytes_post = bpost;
+      plan->groups.push_back(g);
+      offs.push_back(Offs{put(pre.data(), pre.size() * sizeof(MgPass)), put(post.data(), post.size() * sizeof(MgPass)),
+                          put(start.data(), start.size() * sizeof(int)), put(nbx.data(), nbx.size() * sizeof(int))});
+    }
+  }
+  std::vector<CoarsePass> co;
+  for (int w = 0; w < n; w++) {
+    size_t sm = 0;
+    double by = 0.0;
+    co.push_back(coarse_pass(ws[w].d, ws[w].levels, ws[w].nlevels, ws[w].b, &sm, &by));
+    if (sm > plan->coarse_smem) plan->coarse_smem = sm;
+    plan->coarse_bytes += by;
+  }
+  const size_t co_off = put(co.data(), co.size() * sizeof(CoarsePass));
+  if (cudaMalloc(&plan->blob, host.size()) != cudaSuccess) {
+    cudaGetLastError();
+    delete plan;
+    return nullptr;
+  }
+  if (cudaMemcpyAsync(plan->blob, host.data(), host.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(plan->blob);
+    delete plan;
+    return nullptr;
+  }
+  unsigned char* base = static_cast<unsigned char*>(plan->blob);
+  for (size_t i = 0; i < plan->groups.size(); i++) {
+    plan->groups[i].pre = reinterpret_cast<const MgPass*>(base + offs[i].pre);
+    plan->groups[i].post = reinterpret_cast<const MgPass*>(base + offs[i].post);
+    plan->groups[i].start = reinterpret_cast<const int*>(base + offs[i].start);
+    plan->groups[i].nbx = reinterpret_cast<const int*>(base + offs[i].nbx);
+  }
+  plan->coarse = reinterpret_cast<const CoarsePass*>(base + co_off);
+  return plan;
+}
+
+void multigrid_batch_free(MgBatchPlan* plan) {
+  if (!plan) return;
+  if (plan->blob) cudaFree(plan->blob);
+  delete plan;
+}
+
+int multigrid_batch_levels(const MgBatchPlan* plan) { return plan ? plan->levels : 0; }
+
+static void launch_group_pre(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
+  const MgSet set{g.pre, g.start, g.nbx, g.n};
+  const dim3 blk(BX, BY);
+  const char* name = PRE_NAMES[g.level < 7 ? g.level : 7];
+  if (g.small) {
+    const size_t sm = box_smem<32, 16>(2 * c.pre + 1);
+    if (g.level == 0)
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<32, 16, false, true, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
+    else
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<32, 16, false, false, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
+  } else {
+    const size_t sm = box_smem<64, 32>(2 * c.pre + 1);
+    if (g.level == 0)
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<64, 32, false, true, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
+    else
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<64, 32, false, false, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
+  }
+}
+
+static void launch_group_post(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
+  const MgSet set{g.post, g.start, g.nbx, g.n};
+  const dim3 blk(BX, BY);
+  const char* name = POST_NAMES[g.level < 7 ? g.level : 7];
+  if (g.small)
+    RB_LAUNCH(name, g.bytes_post, s,
+              k_mg_post<32, 16, false, MgSet><<<g.total, blk, box_smem<32, 16>(2 * c.post), s>>>(set, c.post));
+  else
+    RB_LAUNCH(name, g.bytes_post, s,
+              k_mg_post<64, 32, false, MgSet><<<g.total, blk, box_smem<64, 32>(2 * c.post), s>>>(set, c.post));
+}
+
+void launch_multigrid_batch(const MgBatchPlan* plan, cudaStream_t s) {
+  set_smem_attrs();
+  const MgConfig& c = plan->c;
+  const int cycles = c.cycles < 1 ? 1 : c.cycles;
+  for (int cy = 0; cy < cycles; cy++) {
+    for (int l = 0; l < plan->levels; l++)
+      for (const MgBatchPlan::Group& g : plan->groups)
+        if (g.level == l) launch_group_pre(g, c, s);
+    RB_LAUNCH("mg_coarse_vcycle", plan->coarse_bytes, s,
+              k_mg_coarse<CoarseMany><<<plan->n, COARSE_THREADS, plan->coarse_smem, s>>>(CoarseMany{plan->coarse, plan->n},
+                                                                                         c.pre, c.post, c.coarse));
+    for (int l = plan->levels - 1; l >= 0; l--)
+      for (const MgBatchPlan::Group& g : plan->groups)
+        if (g.level == l) launch_group_post(g, c, s);
+  }
+}
+
+void launch_multigrid_batch_pre(const MgBatchPlan* plan, int level, cudaStream_t s) {
+  set_smem_attrs();
+  for (const MgBatchPlan::Group& g : plan->groups)
+    if (g.level == level) launch_group_pre(g, plan->c, s);
 }
 
 }  // namespace ribo

@@ -266,4 +266,73 @@ __device__ __forceinline__ float light_absorbed_at(const Dev& d, const ribo_sim_
 // Status words written by kernels instead of trapping.
 enum : uint32_t { ERR_NONE = 0, ERR_TIMEOUT = 1, ERR_BOUNDS = 2 };
 
+// ---- Where a CTA works ------------------------------------------------------
+// Block shapes of the passes, shared by the kernels and by the host code that
+// sizes batched launches.
+constexpr int PASS_BX = 32, PASS_BY = 8;        // per-cell passes: 32x8 cells per CTA
+constexpr int SCATTER_TX = 32, SCATTER_TY = 8;  // transport scatter tile
+constexpr int NET_FLUX_LINES = 32;              // rows or columns per net-flux CTA
+constexpr int LINEAR_THREADS = 256;             // 1-D passes over the environment cells
+constexpr int LEDGER_CELLS_PER_CTA = 16 * LINEAR_THREADS;
+
+// A pass over one world takes the world by value (kernel parameter space).
+// A pass over a batch of worlds takes device tables: the worlds' Dev records
+// and, for the block shape of that pass, the first linear block of every
+// world and its blocks per row; a CTA finds its world by binary search over
+// the block starts (six probes for 64 worlds) and works on one block of that
+// world's grid, so every world gets exactly the CTAs a launch of its own
+// would have.
+struct OneWorld {
+  Dev d;
+  const ribo_sim_params* P;  // this step's parameters
+  uint32_t* out;             // pass-specific output (12 ledger words), or null
+};
+struct WorldSet {
+  const Dev* devs;           // [n]
+  const int* start;          // [n + 1] first linear block of each world
+  const int* nbx;            // [n] blocks per row of each world
+  const ribo_sim_params* P;  // [n] this step's parameters of each world
+  uint32_t* out;             // [n][12] pass-specific output, or null
+  int n;
+};
+struct Cta {
+  uint32_t bx, by;  // block coordinates in the world's grid
+  uint32_t nbx;     // blocks per row of the world's grid
+  int w;            // index of the world in the batch (0 for one world)
+};
+
+__device__ __forceinline__ Cta locate(const OneWorld& s, Dev& d, const ribo_sim_params*& P) {
+  d = s.d;
+  P = s.P;
+  return Cta{blockIdx.x, blockIdx.y, gridDim.x, 0};
+}
+__device__ __forceinline__ int batch_member(const int* __restrict__ start, int n) {
+  const int b = (int)blockIdx.x;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(start + mid) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ Cta locate(const WorldSet& s, Dev& d, const ribo_sim_params*& P) {
+  const int w = batch_member(s.start, s.n);
+  d = s.devs[w];
+  P = s.P + w;
+  const int r = (int)blockIdx.x - __ldg(s.start + w), nb = __ldg(s.nbx + w);
+  return Cta{(uint32_t)(r % nb), (uint32_t)(r / nb), (uint32_t)nb, w};
+}
+__device__ __forceinline__ uint32_t* out_of(const OneWorld& s, int) { return s.out; }
+__device__ __forceinline__ uint32_t* out_of(const WorldSet& s, int w) { return s.out ? s.out + (size_t)w * 12 : nullptr; }
+
+// Opens a pass kernel: the world `d`, its step parameters `P` and the CTA's
+// block coordinates `cta`.
+#define RB_WORLD(sel)                  \
+  Dev d;                               \
+  const ribo_sim_params* P;            \
+  const Cta cta = locate((sel), d, P); \
+  (void)P;                             \
+  (void)cta
+
 }  // namespace ribo

@@ -1,5 +1,6 @@
 // Host-side launchers of the world-step kernels (one per pass).  The world
-// orchestration in world.cu calls them in the reference's dispatch order.
+// orchestration in world.cu and the batch orchestration in batch.cu call
+// them in the reference's dispatch order.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -21,19 +22,71 @@ void ktime_end(cudaStream_t s);
     ::ribo::ktime_end(s);                     \
   } while (0)
 
+// Launch geometries of the passes: how many CTAs one world's grid needs.
+enum Geo : int {
+  GEO_FLUID = 0,    // fluid grid, PASS_BX x PASS_BY cells per CTA
+  GEO_ENV,          // environment grid, PASS_BX x PASS_BY cells per CTA
+  GEO_ENV_LINEAR,   // environment cells, LINEAR_THREADS per CTA (1-D)
+  GEO_SCATTER,      // environment grid, SCATTER_TX x SCATTER_TY tiles
+  GEO_NET_FLUX,     // fluid rows then columns, NET_FLUX_LINES per CTA (1-D)
+  GEO_LEDGER,       // environment cells, LEDGER_CELLS_PER_CTA per CTA (1-D)
+  GEO_COUNT
+};
+void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby);
+
+// Where a pass runs: one world (its Dev by value), or a batch of worlds
+// through device tables (see WorldSet).
+struct Target {
+  Dev one{};
+  const ribo_sim_params* P = nullptr;  // device: the world's params, or [n] params of the batch's step
+  int n = 0;                           // 0: one world; > 0: a batch of n worlds
+  const Dev* devs = nullptr;           // device [n]
+  const int* start[GEO_COUNT] = {};    // device [n + 1] per geometry
+  const int* nbx[GEO_COUNT] = {};      // device [n] per geometry
+  int total[GEO_COUNT] = {};           // CTAs of a batched launch per geometry
+  double fcells = 0.0, cells = 0.0;    // fluid / environment cells over all worlds (byte models)
+  bool batch() const { return n > 0; }
+  WorldSet set(Geo g, uint32_t* out) const { return WorldSet{devs, start[g], nbx[g], P, out, n}; }
+  OneWorld single(uint32_t* out) const { return OneWorld{one, P, out}; }
+  dim3 grid(Geo g) const {
+    int x = 0, y = 0;
+    geo_blocks(g, one, &x, &y);
+    return dim3((unsigned)x, (unsigned)y);
+  }
+};
+Target target_one(const Dev& d, const ribo_sim_params* P);
+
+// Launches pass kernel template `kern` over target `t`: kern<OneWorld> on the
+// world's own grid, or kern<WorldSet> over the CTAs of geometry `geo` of all
+// worlds of the batch.  `out` is the pass-specific output pointer.
+#define RB_PASS(label, bytes, s, t, geo, blk, smem, kern, out, ...)                                             \
+  do {                                                                                                         \
+    if ((t).batch()) {                                                                                         \
+      if ((t).total[geo] > 0)                                                                                  \
+        RB_LAUNCH(label, bytes, s,                                                                             \
+                  kern<WorldSet><<<(unsigned)(t).total[geo], blk, smem, s>>>((t).set(geo, out), ##__VA_ARGS__)); \
+    } else {                                                                                                   \
+      RB_LAUNCH(label, bytes, s, kern<OneWorld><<<(t).grid(geo), blk, smem, s>>>((t).single(out), ##__VA_ARGS__)); \
+    }                                                                                                          \
+  } while (0)
+
+// Velocity ping-pong direction of a pass: reads velocity_a, writes
+// velocity_b (A_TO_B) or the reverse (B_TO_A).
+enum : int { A_TO_B = 0, B_TO_A = 1 };
+
 // fluid.cu
-void launch_solid_mask(const Dev& d, cudaStream_t s);
-void launch_temperature(const Dev& d, const ribo_sim_params* P, cudaStream_t s);
-void launch_forces(const Dev& d, const ribo_sim_params* P, cudaStream_t s);
-void launch_add_forces(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s);
-void launch_diffuse(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s);
-void launch_advect(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s);
-void launch_vorticity(const Dev& d, const ribo_sim_params* P, const float2* vin, float2* vout, cudaStream_t s);
-void launch_divergence(const Dev& d, const float2* vin, cudaStream_t s);
-void launch_subtract_gradient(const Dev& d, const float2* vin, float2* vout, cudaStream_t s);
-void launch_net_flux(const Dev& d, const float2* vin, cudaStream_t s);
-void launch_boundaries(const Dev& d, const float2* vin, float2* vout, cudaStream_t s);
-void launch_smooth(const Dev& d, const float2* vin, cudaStream_t s);
+void launch_solid_mask(const Target& t, cudaStream_t s);
+void launch_temperature(const Target& t, cudaStream_t s);
+void launch_forces(const Target& t, cudaStream_t s);
+void launch_add_forces(const Target& t, int dir, cudaStream_t s);
+void launch_diffuse(const Target& t, int dir, cudaStream_t s);
+void launch_advect(const Target& t, int dir, cudaStream_t s);
+void launch_vorticity(const Target& t, int dir, cudaStream_t s);
+void launch_divergence(const Target& t, int dir, cudaStream_t s);
+void launch_subtract_gradient(const Target& t, int dir, cudaStream_t s);
+void launch_net_flux(const Target& t, int dir, cudaStream_t s);
+void launch_boundaries(const Target& t, int dir, cudaStream_t s);
+void launch_smooth(const Target& t, int dir, cudaStream_t s);
 
 // multigrid.cu
 struct MgLevel {
@@ -74,11 +127,37 @@ void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nlevels, co
                             cudaStream_t s);
 void launch_jacobi(const Dev& d, int iters, cudaStream_t s);
 
+// The fused V-cycles of several worlds advanced together: every fine-level
+// launch covers the tiles of that level in all worlds, and one coarse launch
+// runs one CTA per world.  Built once per batch membership (device tables).
+struct MgWorld {
+  Dev d;  // pressure_a, divergence, mask, status of the world (fixed buffers)
+  const MgLevel* levels;
+  int nlevels;
+  MgBufs b;
+};
+struct MgBatchPlan;
+// Tile shape per fine level index: 0 = by level size (the one-world rule),
+// 1 = 64x32 tiles everywhere, 2 = 32x16 tiles everywhere.
+MgBatchPlan* multigrid_batch_plan(const MgWorld* worlds, int n, const MgConfig& c, const int* tile_mode, int nmodes,
+                                  cudaStream_t s);
+void multigrid_batch_free(MgBatchPlan* plan);
+int multigrid_batch_levels(const MgBatchPlan* plan);  // fine level indices in the plan
+void launch_multigrid_batch(const MgBatchPlan* plan, cudaStream_t s);
+// Pre-smooth launches of one fine level index only (side-effect free: their
+// outputs are rewritten before they are read in the next V-cycle); used to
+// time tile shapes.
+void launch_multigrid_batch_pre(const MgBatchPlan* plan, int level, cudaStream_t s);
+
 // transport.cu
 void launch_slope(const Dev& d, float world_units_per_cell, cudaStream_t s);
-void launch_thermal(const Dev& d, const ribo_sim_params* P, cudaStream_t s);
-void launch_agg(const Dev& d, cudaStream_t s);
-void launch_scatter(const Dev& d, const ribo_sim_params* P, bool simple, cudaStream_t s);
-void launch_ledger(const Dev& d, const uint32_t* chem, uint32_t* out12, cudaStream_t s);
+void launch_thermal(const Target& t, cudaStream_t s);
+void launch_agg(const Target& t, cudaStream_t s);
+void launch_scatter(const Target& t, bool simple, cudaStream_t s);
+// Zeroes chem_next of every world of the target (batched form of the memset).
+void launch_zero_next(const Target& t, cudaStream_t s);
+// Ledger of each world's current chem: 12 words at `out` (one world) or at
+// out + 12 * w (world w of a batch).  The words must be zero beforehand.
+void launch_ledger(const Target& t, uint32_t* out, cudaStream_t s);
 
 }  // namespace ribo

@@ -30,6 +30,10 @@ struct KTimer {
 
 uint64_t ktime_launch_count();
 void ktime_add_launches(uint64_t n);
+// Makes `t` (cleared) the timer of the following launches on this thread, or none.
+void ktime_set_active(KTimer* t);
+// Sums a finished timer's records per kernel name (its stream must be idle).
+ribo_status ktimer_read(const KTimer& t, ribo_kernel_timing* out, uint32_t cap, uint32_t* count);
 
 // A captured step sequence and the ping-pong state it leaves.
 struct GraphEntry {
@@ -45,6 +49,7 @@ struct World {
   ribo_world_settings st{};
   int gw = 0, gh = 0, fw = 0, fh = 0;
   bool fluid_was_on = true;
+  void* batch = nullptr;  // the ribo_batch this world belongs to (its work then runs on the batch's stream)
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   std::vector<void*> allocs;
@@ -116,3 +121,8 @@ struct World {
 };
 
 }  // namespace ribo
+
+// The C handle of a world.
+struct ribo_world {
+  ribo::World w;
+};

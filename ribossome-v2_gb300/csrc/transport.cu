@@ -12,8 +12,7 @@ namespace ribo {
 
 namespace {
 
-constexpr int BX = 32, BY = 8;
-inline dim3 grid2(int w, int h) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY); }
+constexpr int BX = PASS_BX, BY = PASS_BY;
 
 // terrain.wgsl:104-133 (compute_gamma_slope)
 __global__ void k_slope(const __grid_constant__ Dev d, float upc) {
@@ -32,8 +31,10 @@ __global__ void k_slope(const __grid_constant__ Dev d, float upc) {
 }
 
 // transport.wgsl:419-438 (thermal activation, in place; one thread per cell)
-__global__ void k_thermal(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_thermal(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.gw || y >= (uint32_t)d.gh) return;
   uint32_t fx = umin((x * (uint32_t)d.fw) / (uint32_t)d.gw, (uint32_t)d.fw - 1u);
   uint32_t fy = umin((y * (uint32_t)d.fh) / (uint32_t)d.gh, (uint32_t)d.fh - 1u);
@@ -53,15 +54,19 @@ __global__ void k_thermal(const __grid_constant__ Dev d, const ribo_sim_params* 
 }
 
 // transport.wgsl:61-68
-__global__ void k_agg_count(const __grid_constant__ Dev d) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+template <class S>
+__global__ void k_agg_count(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  size_t i = (size_t)cta.bx * blockDim.x + threadIdx.x;
   if (i >= (size_t)d.gw * d.gh) return;
   uint4 c = load_cell(d.chem, i);
   d.agg_act[i] = (c.x & CHEM_STATE_MASK) + (c.y & CHEM_STATE_MASK) + (c.z & CHEM_STATE_MASK) + (c.w & CHEM_STATE_MASK);
 }
 // transport.wgsl:71-87
-__global__ void k_agg_neighbours(const __grid_constant__ Dev d) {
-  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void k_agg_neighbours(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  int x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= d.gw || y >= d.gh) return;
   uint32_t sum = 0;
   for (int dy = -1; dy <= 1; dy++)
@@ -108,8 +113,10 @@ __device__ __forceinline__ float2 smooth_start(uint32_t x0, uint32_t y0, const r
 }
 
 // transport.wgsl:119-406
-__global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
-  uint32_t x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+template <class S>
+__global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   const uint32_t G = d.gw, GH = d.gh;
   if (x >= G || y >= GH) return;
   size_t idx = (size_t)y * G + x;
@@ -322,7 +329,7 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ Dev d, 
 //  C. The accumulator is added to chem_next with one atomic per non-zero
 //     word.
 namespace st {
-constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int TX = SCATTER_TX, TY = SCATTER_TY, NT = TX * TY;
 constexpr int HALO = 2, AW = TX + 2 * HALO, AH = TY + 2 * HALO, AC = AW * AH;
 constexpr uint16_t FAR = 0xFFFFu;  // destination outside the accumulator
 
@@ -342,11 +349,13 @@ struct Smem {
 };
 }  // namespace st
 
-__global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_constant__ Dev d, const ribo_sim_params* __restrict__ P) {
+template <class Sel>
+__global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_constant__ Sel s) {
+  RB_WORLD(s);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   st::Smem& S = *reinterpret_cast<st::Smem*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int X0 = blockIdx.x * st::TX, Y0 = blockIdx.y * st::TY;
+  const int X0 = cta.bx * st::TX, Y0 = cta.by * st::TY;
   const uint32_t G = d.gw, GH = d.gh;
 
   // ---- zero the accumulator, load the blocking flags of tile + ring ----
@@ -692,73 +701,84 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
 
 // ledger.wgsl:225-245: per-block sums in registers and warp shuffles, then
 // one global atomic add per counter (u32, wrapping like the reference).
-__global__ void __launch_bounds__(256) k_ledger(const uint32_t* __restrict__ chem, size_t cells, uint32_t* out) {
-  uint32_t s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const uint4* c4 = reinterpret_cast<const uint4*>(chem);
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += (size_t)gridDim.x * blockDim.x) {
+template <class S>
+__global__ void __launch_bounds__(LINEAR_THREADS) k_ledger(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  uint32_t* out = out_of(s, cta.w);
+  const size_t cells = (size_t)d.gw * d.gh;
+  uint32_t a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const uint4* c4 = reinterpret_cast<const uint4*>(d.chem);
+  const size_t stride = (size_t)cta.nbx * LINEAR_THREADS;
+  for (size_t i = (size_t)cta.bx * LINEAR_THREADS + threadIdx.x; i < cells; i += stride) {
     uint4 c = __ldg(c4 + i);
-    s[0] += c.x & 0xFFFFu;
-    s[1] += c.y & 0xFFFFu;
-    s[2] += c.z & 0xFFFFu;
-    s[3] += c.w & 0xFFFFu;
-    s[4] += c.x >> 16;
-    s[5] += c.y >> 16;
-    s[6] += c.z >> 16;
-    s[7] += c.w >> 16;
+    a[0] += c.x & 0xFFFFu;
+    a[1] += c.y & 0xFFFFu;
+    a[2] += c.z & 0xFFFFu;
+    a[3] += c.w & 0xFFFFu;
+    a[4] += c.x >> 16;
+    a[5] += c.y >> 16;
+    a[6] += c.z >> 16;
+    a[7] += c.w >> 16;
   }
-  __shared__ uint32_t red[8][8];
+  __shared__ uint32_t red[LINEAR_THREADS / 32][8];
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    uint32_t v = s[k];
+    uint32_t v = a[k];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v;
   }
   __syncthreads();
   if (threadIdx.x < 8) {
     uint32_t v = 0;
-    for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++) v += red[wv][threadIdx.x];
+    for (int wv = 0; wv < LINEAR_THREADS / 32; wv++) v += red[wv][threadIdx.x];
     if (v) atomicAdd(out + threadIdx.x, v);
   }
+}
+
+// chem_next = 0 for the next step's scatter (the batched form of a memset).
+template <class S>
+__global__ void __launch_bounds__(LINEAR_THREADS) k_zero_next(const __grid_constant__ S s) {
+  RB_WORLD(s);
+  const size_t i = (size_t)cta.bx * LINEAR_THREADS + threadIdx.x;
+  if (i < (size_t)d.gw * d.gh) reinterpret_cast<uint4*>(d.chem_next)[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 }  // namespace
 
 inline double gc(const Dev& d) { return (double)d.gw * d.gh; }
-inline double fc(const Dev& d) { return (double)d.fw * d.fh; }
 
 void launch_slope(const Dev& d, float upc, cudaStream_t s) {
-  RB_LAUNCH("compute_gamma_slope", 12.0 * gc(d), s, k_slope<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, upc));
+  const dim3 grid((d.gw + BX - 1) / BX, (d.gh + BY - 1) / BY);
+  RB_LAUNCH("compute_gamma_slope", 12.0 * gc(d), s, k_slope<<<grid, dim3(BX, BY), 0, s>>>(d, upc));
 }
-void launch_thermal(const Dev& d, const ribo_sim_params* P, cudaStream_t s) {
-  RB_LAUNCH("thermal_activation", 4.0 * fc(d), s, k_thermal<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, P));
+void launch_thermal(const Target& t, cudaStream_t s) {
+  RB_PASS("thermal_activation", 4.0 * t.fcells, s, t, GEO_ENV, dim3(BX, BY), 0, k_thermal, nullptr);
 }
-void launch_agg(const Dev& d, cudaStream_t s) {
-  size_t cells = (size_t)d.gw * d.gh;
-  RB_LAUNCH("agg_count", 20.0 * gc(d), s, k_agg_count<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(d));
-  RB_LAUNCH("agg_neighbours", 8.0 * gc(d), s, k_agg_neighbours<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d));
+void launch_agg(const Target& t, cudaStream_t s) {
+  RB_PASS("agg_count", 20.0 * t.cells, s, t, GEO_ENV_LINEAR, dim3(LINEAR_THREADS), 0, k_agg_count, nullptr);
+  RB_PASS("agg_neighbours", 8.0 * t.cells, s, t, GEO_ENV, dim3(BX, BY), 0, k_agg_neighbours, nullptr);
 }
-void launch_scatter(const Dev& d, const ribo_sim_params* P, bool simple, cudaStream_t s) {
-  const double bytes = 45.0 * gc(d) + 12.0 * fc(d);
+void launch_scatter(const Target& t, bool simple, cudaStream_t s) {
+  const double bytes = 45.0 * t.cells + 12.0 * t.fcells;
   if (simple) {
-    RB_LAUNCH("transport_scatter_simple", bytes, s, k_scatter<<<grid2(d.gw, d.gh), dim3(BX, BY), 0, s>>>(d, P));
+    RB_PASS("transport_scatter_simple", bytes, s, t, GEO_ENV, dim3(BX, BY), 0, k_scatter, nullptr);
     return;
   }
   static uint64_t attr_done = 0;  // one bit per device
   int dev = 0;
   cudaGetDevice(&dev);
   if (!(attr_done >> (dev & 63) & 1ull)) {
-    cudaFuncSetAttribute(k_scatter_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(st::Smem));
+    cudaFuncSetAttribute(k_scatter_tiled<OneWorld>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(st::Smem));
+    cudaFuncSetAttribute(k_scatter_tiled<WorldSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(st::Smem));
     attr_done |= 1ull << (dev & 63);
   }
-  dim3 grid((d.gw + st::TX - 1) / st::TX, (d.gh + st::TY - 1) / st::TY);
-  RB_LAUNCH("transport_scatter", bytes, s, k_scatter_tiled<<<grid, st::NT, sizeof(st::Smem), s>>>(d, P));
+  RB_PASS("transport_scatter", bytes, s, t, GEO_SCATTER, dim3(st::NT), sizeof(st::Smem), k_scatter_tiled, nullptr);
 }
-void launch_ledger(const Dev& d, const uint32_t* chem, uint32_t* out12, cudaStream_t s) {
-  cudaMemsetAsync(out12, 0, 12 * sizeof(uint32_t), s);
-  size_t cells = (size_t)d.gw * d.gh;
-  unsigned blocks = (unsigned)((cells + 255) / 256);
-  if (blocks > 152u * 8u) blocks = 152u * 8u;
-  RB_LAUNCH("ledger_reduce", 16.0 * gc(d), s, k_ledger<<<blocks, 256, 0, s>>>(chem, cells, out12));
+void launch_zero_next(const Target& t, cudaStream_t s) {
+  RB_PASS("zero_chem_next", 16.0 * t.cells, s, t, GEO_ENV_LINEAR, dim3(LINEAR_THREADS), 0, k_zero_next, nullptr);
+}
+void launch_ledger(const Target& t, uint32_t* out, cudaStream_t s) {
+  RB_PASS("ledger_reduce", 16.0 * t.cells, s, t, GEO_LEDGER, dim3(LINEAR_THREADS), 0, k_ledger, out);
 }
 
 }  // namespace ribo

@@ -71,6 +71,13 @@ void ktime_end(cudaStream_t s) {
 }
 
 uint64_t ktime_launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void ktime_set_active(KTimer* t) {
+  if (t) {
+    t->recs.clear();
+    t->used = 0;
+  }
+  g_active_timer = t;
+}
 void ktime_add_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 cudaEvent_t KTimer::event() {
@@ -285,7 +292,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
     mg.maps = mg_maps.data();
   }
   launch_slope(d, (float)cfg.world_units_per_cell, stream);
-  launch_solid_mask(d, stream);
+  launch_solid_mask(target_one(d, nullptr), stream);
   RB_TRY(cudaGetLastError(), "init kernels");
   RB_TRY(cudaStreamSynchronize(stream), "init");
   return RIBO_OK;
@@ -320,7 +327,7 @@ ribo_status World::upload(ribo_field f, const void* host, size_t bytes) {
   if (f == RIBO_FIELD_GAMMA) {
     Dev d = dev();
     launch_slope(d, (float)cfg.world_units_per_cell, stream);
-    launch_solid_mask(d, stream);
+    launch_solid_mask(target_one(d, nullptr), stream);
     RB_TRY(cudaGetLastError(), "slope/mask");
   }
   RB_TRY(cudaStreamSynchronize(stream), "upload");
@@ -375,33 +382,36 @@ void World::pressure_solve(const Dev& d) {
 void World::record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uint32_t i) {
   uint32_t substep = st.fluid_substep < 1 ? 1 : (st.fluid_substep > 4 ? 4 : st.fluid_substep);
   if (st.fluid_enabled && hp.epoch % substep == 0u) {
-    Dev d = dev();
-    launch_temperature(d, P, stream);  // temp_in -> temp_out
-    std::swap(temp_cur, temp_nxt);     // copy_temperature
+    launch_temperature(target_one(dev(), P), stream);  // temp_in -> temp_out
+    std::swap(temp_cur, temp_nxt);                     // copy_temperature
     std::swap(redox_cur, redox_nxt);
-    d = dev();
-    launch_forces(d, P, stream);                 // buoyancy + gather_forces + clear_force_vectors
-    launch_add_forces(d, P, d.va, d.vb, stream);  // a -> b
-    launch_diffuse(d, P, d.vb, d.va, stream);     // b -> a
-    launch_advect(d, P, d.va, d.vb, stream);      // a -> b
-    launch_vorticity(d, P, d.vb, d.va, stream);   // b -> a
-    launch_divergence(d, d.va, stream);
-    pressure_solve(d);
-    launch_subtract_gradient(d, d.va, d.vb, stream);  // a -> b
-    launch_net_flux(d, d.vb, stream);
-    launch_boundaries(d, d.vb, d.va, stream);  // b -> a (final in a)
-    launch_smooth(d, d.va, stream);
-    launch_thermal(d, P, stream);
+    const Target t = target_one(dev(), P);
+    launch_forces(t, stream);                // buoyancy + gather_forces + clear_force_vectors
+    launch_add_forces(t, A_TO_B, stream);
+    launch_diffuse(t, B_TO_A, stream);
+    launch_advect(t, A_TO_B, stream);
+    launch_vorticity(t, B_TO_A, stream);
+    launch_divergence(t, A_TO_B, stream);    // reads velocity_a
+    pressure_solve(t.one);
+    launch_subtract_gradient(t, A_TO_B, stream);
+    launch_net_flux(t, B_TO_A, stream);      // reads velocity_b
+    launch_boundaries(t, B_TO_A, stream);    // final velocity in velocity_a
+    launch_smooth(t, A_TO_B, stream);        // reads velocity_a
+    launch_thermal(t, stream);
   }
   uint32_t te = hp.transport_every < 1 ? 1 : hp.transport_every;
   if (hp.epoch % te == 0u) {
-    Dev d = dev();
-    if (hp.aggregation > 0.0f) launch_agg(d, stream);
-    launch_scatter(d, P, st.transport_simple != 0, stream);
+    const Target t = target_one(dev(), P);
+    if (hp.aggregation > 0.0f) launch_agg(t, stream);
+    launch_scatter(t, st.transport_simple != 0, stream);
     std::swap(chem_cur, chem_nxt);  // transport_commit
     cudaMemsetAsync(chem_nxt, 0, cells() * 16, stream);
   }
-  if (st.ledger_each_step) launch_ledger(dev(), chem_cur, step_ledgers + (size_t)i * 12, stream);
+  if (st.ledger_each_step) {
+    uint32_t* out = step_ledgers + (size_t)i * 12;
+    cudaMemsetAsync(out, 0, 12 * sizeof(uint32_t), stream);
+    launch_ledger(target_one(dev(), nullptr), out, stream);
+  }
 }
 
 ribo_status World::step(const ribo_sim_params* per_step, uint32_t n) {
@@ -426,11 +436,9 @@ ribo_status World::step(const ribo_sim_params* per_step, uint32_t n) {
   RB_TRY(cudaMemcpyAsync(ds, hs, n * sizeof(ribo_sim_params), cudaMemcpyHostToDevice, stream), "params");
   RB_TRY(cudaEventRecord(param_ev[slot], stream), "event");
   if (timing) {
-    timer.recs.clear();
-    timer.used = 0;
-    g_active_timer = &timer;
+    ktime_set_active(&timer);
     for (uint32_t i = 0; i < n; i++) record_step(per_step[i], ds + i, i);
-    g_active_timer = nullptr;
+    ktime_set_active(nullptr);
   } else {
     ribo_status s = record_steps_graphed(per_step, ds, n, slot);
     if (s != RIBO_OK) return s;
@@ -522,6 +530,10 @@ ribo_status World::record_steps_graphed(const ribo_sim_params* per_step, const r
 ribo_status World::read_timing(ribo_kernel_timing* out, uint32_t cap, uint32_t* count) {
   RB_TRY(bind(), "device");
   RB_TRY(cudaStreamSynchronize(stream), "timing");
+  return ktimer_read(timer, out, cap, count);
+}
+
+ribo_status ktimer_read(const KTimer& timer, ribo_kernel_timing* out, uint32_t cap, uint32_t* count) {
   std::vector<ribo_kernel_timing> agg;
   for (const KTimer::Rec& r : timer.recs) {
     float ms = 0.0f;
@@ -561,7 +573,8 @@ ribo_status World::check_status() {
 
 ribo_status World::ledger_read(uint32_t out[12]) {
   RB_TRY(bind(), "device");
-  launch_ledger(dev(), chem_cur, ledger, stream);
+  RB_TRY(cudaMemsetAsync(ledger, 0, 12 * sizeof(uint32_t), stream), "ledger");
+  launch_ledger(target_one(dev(), nullptr), ledger, stream);
   RB_TRY(cudaGetLastError(), "ledger");
   RB_TRY(cudaMemcpyAsync(out, ledger, 12 * 4, cudaMemcpyDeviceToHost, stream), "ledger");
   RB_TRY(cudaStreamSynchronize(stream), "ledger");
@@ -580,10 +593,6 @@ using ribo::set_error;
 // C ABI
 
 extern "C" {
-
-struct ribo_world {
-  ribo::World w;
-};
 
 const char* ribo_last_error(void) { return ribo::g_last_error.c_str(); }
 
@@ -655,7 +664,10 @@ ribo_status ribo_world_create(const ribo_world_cfg* cfg, ribo_world** out) {
   return RIBO_OK;
 }
 
-void ribo_world_destroy(ribo_world* w) { delete w; }
+void ribo_world_destroy(ribo_world* w) {
+  if (w && w->w.batch) ribo_batch_remove(static_cast<ribo_batch*>(w->w.batch), w);
+  delete w;
+}
 
 ribo_status ribo_world_set_settings(ribo_world* w, const ribo_world_settings* s) {
   if (!w || !s) return set_error(RIBO_INVALID_ARG, "null argument");

@@ -116,6 +116,21 @@ def load_library(path: str = LIB_PATH):
         "ribo_world_step_ledgers": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
         "ribo_world_mark": ([vp, ctypes.c_uint32], ctypes.c_int),
         "ribo_world_elapsed_ms": ([vp, ctypes.c_uint32, ctypes.c_uint32, P(ctypes.c_float)], ctypes.c_int),
+        "ribo_batch_create": ([ctypes.c_uint32, P(vp)], ctypes.c_int),
+        "ribo_batch_destroy": ([vp], None),
+        "ribo_batch_add": ([vp, vp], ctypes.c_int),
+        "ribo_batch_remove": ([vp, vp], ctypes.c_int),
+        "ribo_batch_size": ([vp], ctypes.c_uint32),
+        "ribo_batch_step": ([vp, P(SimParams), ctypes.c_uint32], ctypes.c_int),
+        "ribo_batch_encode_steps": ([vp, P(SimParams), ctypes.c_uint32], ctypes.c_int),
+        "ribo_batch_step_ledgers": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
+        "ribo_batch_sync": ([vp], ctypes.c_int),
+        "ribo_batch_mark": ([vp, ctypes.c_uint32], ctypes.c_int),
+        "ribo_batch_elapsed_ms": ([vp, ctypes.c_uint32, ctypes.c_uint32, P(ctypes.c_float)], ctypes.c_int),
+        "ribo_batch_autotune": ([vp, P(ctypes.c_uint32)], ctypes.c_int),
+        "ribo_batch_set_tile_modes": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
+        "ribo_batch_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "ribo_batch_read_kernel_timing": ([vp, P(KernelTiming), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -331,3 +346,116 @@ class World:
         for f in (GAMMA, CHEM, LIGHT, VELOCITY, PRESSURE, TEMP, REDOX, HEAT, SHADE, FORCE_VECTORS, REDOX_EATEN):
             if f in inputs:
                 self.upload(f, inputs[f])
+
+
+class Batch:
+    """Worlds advanced in lock step: every pass is one launch over all members.
+
+    Members keep their own state and settings (World.settings is pushed to
+    the library at every step call); each member's results are the bits it
+    would get stepped alone with the same parameters.
+    """
+
+    def __init__(self, worlds=(), device: int = 0):
+        lib = load_library()
+        h = ctypes.c_void_p()
+        check(lib.ribo_batch_create(device, ctypes.byref(h)), "ribo_batch_create")
+        self._h = h
+        self._lib = lib
+        self.worlds = []
+        for w in worlds:
+            self.add(w)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ribo_batch_destroy(self._h)
+            self._h = None
+            self.worlds = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return len(self.worlds)
+
+    def add(self, w: World):
+        check(self._lib.ribo_batch_add(self._h, w._h), "ribo_batch_add")
+        self.worlds.append(w)
+
+    def remove(self, w: World):
+        check(self._lib.ribo_batch_remove(self._h, w._h), "ribo_batch_remove")
+        self.worlds.remove(w)
+
+    def _sync_settings(self):
+        for w in self.worlds:
+            w._sync_settings()
+
+    def step(self, per_world_steps):
+        """per_world_steps[k] = the k-th member's list of per-step SimParams (same length for all)."""
+        self._sync_settings()
+        n = len(per_world_steps[0]) if per_world_steps else 0
+        flat = [p for steps in per_world_steps for p in steps]
+        assert len(flat) == n * len(self.worlds)
+        arr = (SimParams * len(flat))(*flat)
+        check(self._lib.ribo_batch_step(self._h, arr, n), "ribo_batch_step")
+
+    def encode_steps(self, steps: int):
+        """ribo_world_encode_steps for every member, advancing each member's params.epoch."""
+        self._sync_settings()
+        arr = (SimParams * len(self.worlds))(*[w.params for w in self.worlds])
+        check(self._lib.ribo_batch_encode_steps(self._h, arr, steps), "ribo_batch_encode_steps")
+        for w, p in zip(self.worlds, arr):
+            w.params = p.copy()
+
+    def run(self, steps: int):
+        done = 0
+        while done < steps:
+            n = min(MAX_STEPS_PER_FRAME, steps - done)
+            self.encode_steps(n)
+            done += n
+
+    def step_ledgers(self, n: int):
+        """[member][step] Ledger after each of the last call's n steps."""
+        N = len(self.worlds)
+        out = (ctypes.c_uint32 * (12 * n * N))()
+        check(self._lib.ribo_batch_step_ledgers(self._h, out, n), "batch step ledgers")
+        return [[Ledger.from_words(out[12 * (k * n + i):12 * (k * n + i) + 12]) for i in range(n)] for k in range(N)]
+
+    def sync(self):
+        check(self._lib.ribo_batch_sync(self._h), "batch sync")
+
+    def mark(self, slot: int):
+        check(self._lib.ribo_batch_mark(self._h, slot), "mark")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = ctypes.c_float()
+        check(self._lib.ribo_batch_elapsed_ms(self._h, a, b, ctypes.byref(ms)), "elapsed")
+        return ms.value
+
+    def autotune(self):
+        modes = (ctypes.c_uint32 * 8)()
+        check(self._lib.ribo_batch_autotune(self._h, modes), "autotune")
+        return list(modes)
+
+    def set_tile_modes(self, modes):
+        arr = (ctypes.c_uint32 * len(modes))(*modes)
+        check(self._lib.ribo_batch_set_tile_modes(self._h, arr, len(modes)), "tile modes")
+
+    def enable_kernel_timing(self, on: bool = True):
+        check(self._lib.ribo_batch_enable_kernel_timing(self._h, 1 if on else 0), "kernel timing")
+
+    def read_kernel_timing(self):
+        cap = 128
+        arr = (KernelTiming * cap)()
+        n = ctypes.c_uint32()
+        check(self._lib.ribo_batch_read_kernel_timing(self._h, arr, cap, ctypes.byref(n)), "read timing")
+        return [(arr[i].name.decode(), arr[i].launches, arr[i].ms, arr[i].bytes) for i in range(min(n.value, cap))]

@@ -121,3 +121,19 @@ def bench_params(seed: int = 1000) -> "rw.SimParams":
     p.transport_every = 1
     p.day_period = 0.0
     return p
+
+
+# The batched workload: worlds of uneven sizes drawn by seed from these
+# grids (square sides, then two rectangles), each with its own noise seed,
+# obstacle fraction U(0.05, 0.25) and monomer mean U(1, 8).
+BATCH_GRIDS = [(s, s) for s in (128, 192, 256, 384, 512, 768, 1024)] + [(512, 2048), (2048, 256)]
+
+
+def batch_specs(n: int = 64, seed: int = 7):
+    """[(grid (w, h), noise seed, rock_frac, monomer_mean)] of the batched workload."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        g = BATCH_GRIDS[int(rng.integers(len(BATCH_GRIDS)))]
+        out.append((g, 1000 + i, float(rng.uniform(0.05, 0.25)), float(rng.uniform(1.0, 8.0))))
+    return out

@@ -94,3 +94,22 @@ def test_create_without_gpu_reports_cuda_error(rw):
     with pytest.raises(rw.RiboError) as e:
         rw.World(32)
     assert "CUDA_ERROR" in str(e.value)
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-GPU error path")
+def test_batch_without_gpu_reports_cuda_error(rw):
+    with pytest.raises(rw.RiboError) as e:
+        rw.Batch()
+    assert "CUDA_ERROR" in str(e.value)
+
+
+def test_batch_null_arguments_are_rejected(rw):
+    lib = rw.load_library()
+    assert lib.ribo_batch_create(0, None) == 1
+    assert lib.ribo_batch_add(None, None) == 1
+    assert lib.ribo_batch_remove(None, None) == 1
+    assert lib.ribo_batch_step(None, None, 1) == 1
+    assert lib.ribo_batch_encode_steps(None, None, 1) == 1
+    assert lib.ribo_batch_set_tile_modes(None, None, 0) == 1
+    assert lib.ribo_batch_size(None) == 0
+    lib.ribo_batch_destroy(None)
