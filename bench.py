@@ -18,6 +18,12 @@ transport + ledger) of one world.
   --impl reference   the CPU restatement of the reference's passes (the
          reference itself is Rust + WGSL on wgpu and cannot run here),
          all host threads, bounded sample of the same workload
+  batched  (N = 1) 64 worlds of uneven sizes as one ribo_batch vs the same
+         worlds stepped one after another: world-steps/s and p50/p99 step
+         latency of each form
+  serving  (N = 1) the continuous-batching server fed by a Poisson request
+         stream (200 req/s for 60 s, 150 GB budget), and again at a rate the
+         GPU sustains: world-steps/s, p50/p99 step and job latency
 N > 1 GPUs run independent replicas (one world per rank, no collective).
 """
 import argparse
@@ -366,13 +372,15 @@ def run_ours(args):
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(n)
-    if not args.no_batched:
+    # batched and served forms: single-GPU runs only (replicas would repeat them per rank)
+    if ws == 1 and not args.no_batched:
         w.close()
-        bt = run_batched(args, local)
-        if ws > 1:  # replicas: every rank runs its own batch; whole-job throughput sums them
-            bt["batched"]["world_steps_per_s"] = sum_over_ranks(ws, bt["batched"]["world_steps_per_s"])
-            bt["plain"]["world_steps_per_s"] = sum_over_ranks(ws, bt["plain"]["world_steps_per_s"])
-        line["batched"] = bt
+        line["batched"] = run_batched(args, local)
+    if ws == 1 and not args.no_serving:
+        line["serving"] = run_serving(args, local, args.serve_rate, args.serve_seconds, args.serve_drain_seconds)
+        if args.serve_sustainable_rate > 0:
+            line["serving_sustainable"] = run_serving(args, local, args.serve_sustainable_rate,
+                                                      args.serve_sustainable_seconds, args.serve_sustainable_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -485,6 +493,115 @@ def run_batched(args, local):
     }
 
 
+def serving_trace(rate, seconds, seed=11):
+    """Poisson arrivals; each request: a world of log-uniform side 128..2048
+    with aspect ratio up to 4:1 (sides rounded to multiples of 32) and a
+    log-uniform step count in 10..1000."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= seconds:
+            return out
+        side = float(np.exp(rng.uniform(np.log(128), np.log(2048))))
+        aspect = float(np.exp(rng.uniform(-np.log(4), np.log(4))))
+        w = int(min(2048, max(128, round(side * np.sqrt(aspect) / 32) * 32)))
+        h = int(min(2048, max(128, round(side / np.sqrt(aspect) / 32) * 32)))
+        steps = int(round(float(np.exp(rng.uniform(np.log(10), np.log(1000))))))
+        out.append((t, (w, h), steps, len(out)))
+
+
+def run_serving(args, local, rate, seconds, drain_seconds):
+    """Continuous-batching server fed by a Poisson request stream in real time.
+
+    Each request's fields are a seeded crop of one of two pre-generated
+    2048x2048 input sets (same generators and distributions as the plain
+    workload: value-noise velocity, 10% rock, Poisson(4) monomers); the
+    request becomes a job (materialised, copied, queued on the server) when
+    the server's own queue is short, and its latency counts from its arrival.
+    The server admits jobs in arrival order against the HBM budget, keeps
+    their state resident and advances all resident jobs together each
+    iteration.  The run stops taking arrivals after `serve_seconds`, then
+    runs the iterations it has time for within `drain_seconds`.
+    """
+    import numpy as np
+    import ribo_world as rw
+    import synth
+
+    trace = serving_trace(rate, seconds)
+    templates = [synth.make_world_inputs(2048, seed=5000 + k) for k in range(2)]
+    fields = (rw.GAMMA, rw.CHEM, rw.VELOCITY, rw.LIGHT)
+
+    def job_inputs(i, w, h):
+        rng = np.random.default_rng(90000 + i)
+        tp = templates[i % len(templates)]
+        x0 = int(rng.integers(0, 2048 - w + 1)) // 2 * 2
+        y0 = int(rng.integers(0, 2048 - h + 1)) // 2 * 2
+        return {
+            rw.GAMMA: tp[rw.GAMMA][y0:y0 + h, x0:x0 + w],
+            rw.CHEM: tp[rw.CHEM][y0:y0 + h, x0:x0 + w],
+            rw.VELOCITY: tp[rw.VELOCITY][y0:y0 + h, x0:x0 + w],
+            rw.LIGHT: tp[rw.LIGHT][:, y0 // 2:(y0 + h) // 2, x0 // 2:(x0 + w) // 2],
+        }
+
+    settings = rw.default_settings()
+    settings.fluid_substep = 1
+    settings.mg_cycles = 4
+    budget = int(args.serve_budget_gb * 1e9)
+    srv = rw.Server(budget, max_chunk_steps=args.serve_chunk, device=local)
+    t0 = time.perf_counter()
+    arrival = {}
+    nxt = 0
+    it_records = []
+    while True:
+        now = time.perf_counter() - t0
+        if now > seconds + drain_seconds:
+            break
+        st = srv.stats()
+        while nxt < len(trace) and trace[nxt][0] <= min(now, seconds) and st.pending < args.serve_queue:
+            ta, (w, h), steps, i = trace[nxt]
+            jid = srv.submit((w, h), steps=steps, params=synth.bench_params(7000 + i), settings=settings,
+                             inputs=job_inputs(i, w, h), mg_min_size=16, mg_pre=3, mg_post=3, user_tag=i)
+            arrival[jid] = ta
+            nxt += 1
+            st = srv.stats()
+        if st.active == 0 and st.pending == 0:
+            if nxt >= len(trace):
+                break
+            time.sleep(min(0.01, max(0.0, trace[nxt][0] - now)))
+            continue
+        srv.iterate()
+        it_records += srv.iterations()
+    wall = time.perf_counter() - t0
+    results = srv.results()
+    it_records += srv.iterations()
+    st = srv.stats()
+    done = [r for r, _ in results if r.status == 0]
+    job_lat = [(r.t_done_ms / 1000.0 - arrival[r.id]) * 1000.0 for r in done]
+    job_step_lat = [l / r.steps for l, r in zip(job_lat, done)]
+    per_step = []
+    for ms, steps, active in it_records:
+        per_step += [ms / max(steps, 1)] * max(active, 1)  # one sample per resident job-step
+    srv.close()
+    return {
+        "workload": f"Poisson arrivals at {rate:g} req/s for {seconds:g} s; world side "
+                    f"log-uniform 128..2048, aspect up to 4:1, steps log-uniform 10..1000; "
+                    f"{args.serve_budget_gb:g} GB HBM budget; chunks of {args.serve_chunk} steps",
+        "requests_arrived": len(trace), "submitted": st.submitted, "admitted": st.admitted,
+        "completed": st.completed, "resident_at_end": st.active, "queued_at_end": st.pending,
+        "not_yet_submitted": len(trace) - nxt,
+        "world_steps": st.world_steps, "gpu_ms": st.gpu_ms, "wall_s": wall,
+        "world_steps_per_s": st.world_steps / wall, "world_steps_per_gpu_s": st.world_steps / max(st.gpu_ms / 1000.0, 1e-9),
+        "step_latency_ms_p50": percentile(per_step, 50), "step_latency_ms_p99": percentile(per_step, 99),
+        "job_latency_ms_p50": percentile(job_lat, 50), "job_latency_ms_p99": percentile(job_lat, 99),
+        "job_ms_per_step_p50": percentile(job_step_lat, 50), "job_ms_per_step_p99": percentile(job_step_lat, 99),
+        "iterations": st.iterations,
+        "note": "offered load ~= rate x E[cells x steps]; latencies of completed jobs count from arrival",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -500,6 +617,15 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=200)
     ap.add_argument("--latency-samples", type=int, default=5)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-drain-seconds", type=float, default=0.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-chunk", type=int, default=16)
+    ap.add_argument("--serve-queue", type=int, default=4)
+    ap.add_argument("--serve-sustainable-rate", type=float, default=6.0)
+    ap.add_argument("--serve-sustainable-seconds", type=float, default=40.0)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

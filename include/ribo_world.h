@@ -228,6 +228,12 @@ void ribo_world_settings_default(ribo_world_settings* out);
 ribo_status ribo_world_create(const ribo_world_cfg* cfg, ribo_world** out);
 void ribo_world_destroy(ribo_world* w);
 
+// Device bytes ribo_world_create allocates for `cfg` (no counterpart in the
+// reference; admission control of ribo_server uses it), and the bytes a
+// created world holds.  No GPU needed for the first.
+ribo_status ribo_world_footprint(const ribo_world_cfg* cfg, uint64_t* bytes);
+ribo_status ribo_world_memory(const ribo_world* w, uint64_t* bytes);
+
 ribo_status ribo_world_set_settings(ribo_world* w, const ribo_world_settings* s);
 ribo_status ribo_world_get_settings(const ribo_world* w, ribo_world_settings* out);
 
@@ -328,6 +334,10 @@ uint32_t ribo_batch_size(const ribo_batch* b);
 // stream.  per_step[k * n + i] holds the parameters of step i of the k-th
 // member (membership order: the order of ribo_batch_add, less removals).
 ribo_status ribo_batch_step(ribo_batch* b, const ribo_sim_params* per_step, uint32_t n);
+// As ribo_batch_step, but member k runs only the first member_steps[k] (<= n)
+// of its n entries; the others leave it untouched.
+ribo_status ribo_batch_step_ragged(ribo_batch* b, const ribo_sim_params* per_step, uint32_t n,
+                                   const uint32_t* member_steps);
 // ribo_world_encode_steps for every member: params[k] is the k-th member's
 // SimParams; the per-step copies are derived from it with that member's
 // settings, and params[k].epoch advances by `n`.
@@ -355,6 +365,83 @@ ribo_status ribo_batch_set_tile_modes(ribo_batch* b, const uint32_t* modes, uint
 // Per-kernel timing of the next ribo_batch_step calls (as for a world).
 ribo_status ribo_batch_enable_kernel_timing(ribo_batch* b, int enable);
 ribo_status ribo_batch_read_kernel_timing(ribo_batch* b, ribo_kernel_timing* out, uint32_t cap, uint32_t* count);
+
+// ---- Serving: world-step jobs with continuous batching ----------------------
+// No counterpart in the reference.  A server keeps a FIFO of submitted jobs
+// (a world, its settings and SimParams, a step count, its initial fields)
+// and a batch of resident worlds.  Each iteration (1) retires the jobs that
+// have run all their steps -- reads their results into the caller's
+// buffers, frees their worlds --, (2) admits queued jobs in arrival order
+// while their device footprint fits the HBM budget (and the resident
+// count stays under max_active), creating and uploading their worlds, and
+// (3) advances every resident job by up to max_chunk_steps steps in one
+// ragged batched call (a job never runs past its step count).  Jobs that
+// arrive while others run join at the next iteration: their work overlaps
+// with the others' in the same launches.  A job's results are the same bits
+// as when its world is stepped alone with ribo_world_encode_steps.
+typedef struct ribo_server ribo_server;
+
+typedef struct ribo_server_cfg {
+  uint32_t device;
+  uint32_t max_chunk_steps;   // steps per iteration (1..64)
+  uint32_t max_active;        // resident jobs at most (0 = limited by the budget only)
+  uint32_t reserved0;
+  uint64_t hbm_budget_bytes;  // device bytes the resident worlds may hold (ribo_world_footprint)
+  uint64_t reserved[2];
+} ribo_server_cfg;
+
+typedef struct ribo_job {
+  ribo_world_cfg world;
+  ribo_world_settings settings;
+  ribo_sim_params params;  // the base SimParams; per-step copies as ribo_world_encode_steps derives them
+  uint32_t steps;          // steps to run (>= 1)
+  uint32_t reserved0;
+  uint64_t user_tag;
+  // Initial fields (host memory, ribo_world_upload sizes; null = zero),
+  // copied by ribo_server_submit.  GAMMA is uploaded first.
+  const void* inputs[RIBO_FIELD_COUNT];
+  // Result fields: host buffers of ribo_world_read sizes, filled when the job
+  // retires (null = not read).  They must stay valid until then.
+  void* outputs[RIBO_FIELD_COUNT];
+} ribo_job;
+
+typedef struct ribo_job_result {
+  uint64_t id;
+  uint64_t user_tag;
+  int32_t status;          // ribo_status of the job
+  uint32_t steps;
+  uint32_t ledger[12];     // ledger of the final state
+  uint64_t device_bytes;   // footprint the job held while resident
+  double t_submit_ms;      // host clock, ms since the server was created
+  double t_admit_ms;
+  double t_done_ms;        // when the iteration that retired it observed its last step done
+} ribo_job_result;
+
+typedef struct ribo_server_stats {
+  uint64_t submitted, admitted, completed, pending, active;
+  uint64_t bytes_in_use;   // footprint of the resident worlds
+  uint64_t world_steps;    // job steps run so far
+  uint64_t iterations;
+  double gpu_ms;           // device time of the batched calls so far
+} ribo_server_stats;
+
+ribo_status ribo_server_create(const ribo_server_cfg* cfg, ribo_server** out);
+// Destroys the server and every world it holds; results not yet taken are lost.
+void ribo_server_destroy(ribo_server* s);
+// Queues a job; its id is written to *id.  RIBO_OVER_BUDGET when the job's
+// footprint alone exceeds the budget, RIBO_INVALID_ARG on a bad job.
+ribo_status ribo_server_submit(ribo_server* s, const ribo_job* job, uint64_t* id);
+// One iteration (retire, admit, advance); *active = resident jobs after it.
+ribo_status ribo_server_iterate(ribo_server* s, uint32_t* active);
+// Iterates until no job is queued or resident.
+ribo_status ribo_server_drain(ribo_server* s);
+// Moves up to `cap` finished results to `out` (oldest first); *n = moved.
+ribo_status ribo_server_results(ribo_server* s, ribo_job_result* out, uint32_t cap, uint32_t* n);
+ribo_status ribo_server_get_stats(const ribo_server* s, ribo_server_stats* out);
+// Per-iteration records since the last call (oldest first, at most cap):
+// device ms of the iteration's batched call, its steps and resident jobs.
+ribo_status ribo_server_iterations(ribo_server* s, float* ms, uint32_t* steps, uint32_t* active, uint32_t cap,
+                                   uint32_t* n);
 
 // Allocation-free multigrid pressure solve.  No counterpart in the reference:
 // it exists for callers that cannot allocate device memory while they run

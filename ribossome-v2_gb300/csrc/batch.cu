@@ -173,7 +173,7 @@ struct Batch {
   Target target(Group* g, const ribo_sim_params* P);
   void plan_mg(Group* g);
   ribo_status ensure_capacity();
-  ribo_status step(const ribo_sim_params* per_step, uint32_t n);
+  ribo_status step(const ribo_sim_params* per_step, uint32_t n, const uint32_t* member_steps);
   void record_step(const std::vector<StepUse>& uses, const ribo_sim_params* P0, uint32_t i);
   std::string graph_key(const std::vector<std::vector<StepUse>>& plan, uint32_t n, int slot) const;
   ribo_status record_graphed(const std::vector<std::vector<StepUse>>& plan, const ribo_sim_params* P0, uint32_t n,
@@ -486,10 +486,13 @@ ribo_status Batch::record_graphed(const std::vector<std::vector<StepUse>>& plan,
   return RIBO_OK;
 }
 
-ribo_status Batch::step(const ribo_sim_params* per_step, uint32_t n) {
+ribo_status Batch::step(const ribo_sim_params* per_step, uint32_t n, const uint32_t* member_steps) {
   if (n == 0 || worlds.empty()) return RIBO_OK;
   if (!per_step) return set_error(RIBO_INVALID_ARG, "null params");
   if (n > MAX_STEPS) return set_error(RIBO_INVALID_ARG, "%u steps per call (at most %u)", n, MAX_STEPS);
+  if (member_steps)
+    for (size_t k = 0; k < worlds.size(); k++)
+      if (member_steps[k] > n) return set_error(RIBO_INVALID_ARG, "member %zu: %u steps of %u", k, member_steps[k], n);
   RB_TRY(bind(), "device");
   {
     ribo_status s = ensure_capacity();
@@ -522,6 +525,7 @@ ribo_status Batch::step(const ribo_sim_params* per_step, uint32_t n) {
     std::vector<std::vector<int>> members;
     std::vector<uint32_t> scheds;
     for (size_t k = 0; k < N; k++) {
+      if (member_steps && i >= member_steps[k]) continue;
       const ribo_sim_params& p = per_step[k * n + i];
       const uint32_t sb = sched_bits(*worlds[k], p);
       const std::string ck = class_key(*worlds[k], sb);
@@ -714,7 +718,13 @@ uint32_t ribo_batch_size(const ribo_batch* b) { return b ? (uint32_t)b->b.worlds
 
 ribo_status ribo_batch_step(ribo_batch* b, const ribo_sim_params* per_step, uint32_t n) {
   if (!b) return set_error(RIBO_INVALID_ARG, "null batch");
-  return b->b.step(per_step, n);
+  return b->b.step(per_step, n, nullptr);
+}
+
+ribo_status ribo_batch_step_ragged(ribo_batch* b, const ribo_sim_params* per_step, uint32_t n,
+                                   const uint32_t* member_steps) {
+  if (!b || !member_steps) return set_error(RIBO_INVALID_ARG, "null argument");
+  return b->b.step(per_step, n, member_steps);
 }
 
 ribo_status ribo_batch_encode_steps(ribo_batch* b, ribo_sim_params* params, uint32_t n) {
@@ -727,7 +737,7 @@ ribo_status ribo_batch_encode_steps(ribo_batch* b, ribo_sim_params* params, uint
     ribo_status st = ribo_derive_step_params(&params[k], &b->b.worlds[k]->st, n, &buf[k * n]);
     if (st != RIBO_OK) return st;
   }
-  ribo_status st = b->b.step(buf.data(), n);
+  ribo_status st = b->b.step(buf.data(), n, nullptr);
   if (st != RIBO_OK) return st;
   for (size_t k = 0; k < N; k++) {
     const ribo_world_settings& s = b->b.worlds[k]->st;

@@ -28,6 +28,11 @@ struct KTimer {
   ~KTimer();
 };
 
+// Device bytes a world with configuration `c` allocates (defaults applied).
+size_t world_footprint(const ribo_world_cfg& c);
+// Bytes of field `f` of a world with configuration `c` (0: no such field).
+size_t field_bytes_of(const ribo_world_cfg& c, ribo_field f);
+
 uint64_t ktime_launch_count();
 void ktime_add_launches(uint64_t n);
 // Makes `t` (cleared) the timer of the following launches on this thread, or none.
@@ -81,6 +86,7 @@ struct World {
   // multigrid
   std::vector<MgLevel> levels;
   size_t mg_total = 0;
+  size_t device_bytes = 0;  // sum of the world's device buffers
   MgBufs mg{};
   std::vector<MgLevelMaps> mg_maps;
   uint32_t* status = nullptr;  // kernel error bits (RIBO_ERR_*)

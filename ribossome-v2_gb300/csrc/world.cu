@@ -93,8 +93,12 @@ KTimer::~KTimer() {
   for (cudaEvent_t e : pool) cudaEventDestroy(e);
 }
 
-size_t World::field_bytes(ribo_field f) const {
-  size_t C = cells(), F = fcells(), L = lcells();
+size_t World::field_bytes(ribo_field f) const { return field_bytes_of(cfg, f); }
+
+size_t field_bytes_of(const ribo_world_cfg& c, ribo_field f) {
+  const size_t C = (size_t)c.grid_w * c.grid_h, F = (size_t)c.fluid_w * c.fluid_h;
+  const size_t L = (size_t)(c.grid_w / 2) * (c.grid_h / 2);
+  const size_t fw = c.fluid_w, fh = c.fluid_h;
   switch (f) {
     case RIBO_FIELD_CHEM: return C * 16;
     case RIBO_FIELD_GAMMA: return C * 4;
@@ -110,7 +114,7 @@ size_t World::field_bytes(ribo_field f) const {
     case RIBO_FIELD_DIVERGENCE: return F * 4;
     case RIBO_FIELD_FORCE_VECTORS: return F * 8;
     case RIBO_FIELD_REDOX_EATEN: return F * 4;
-    case RIBO_FIELD_NET_FLUX: return ((size_t)fw + fh) * 4;
+    case RIBO_FIELD_NET_FLUX: return (fw + fh) * 4;
     case RIBO_FIELD_SHADE: return 2 * L * 4;
     default: return 0;
   }
@@ -187,12 +191,65 @@ Dev World::dev() const {
   return d;
 }
 
+// World buffers come from the device's stream-ordered pool: creating and
+// destroying worlds (a server admits and retires them continuously) then
+// neither synchronises the device nor returns memory to the driver.
 ribo_status World::alloc(void** p, size_t bytes, const char* what) {
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaError_t e = cudaMallocAsync(p, bytes, own_stream);
   if (e != cudaSuccess) return cuda_status(e, what);
   allocs.push_back(*p);
-  e = cudaMemsetAsync(*p, 0, bytes, stream);
+  device_bytes += bytes;
+  e = cudaMemsetAsync(*p, 0, bytes, own_stream);
   return cuda_status(e, what);
+}
+
+static void keep_pool_memory(int dev) {
+  static uint64_t done = 0;  // one bit per device
+  if (done >> (dev & 63) & 1ull) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
+  done |= 1ull << (dev & 63);
+}
+
+// Multigrid levels (src/world/mod.rs:637-671): halve while both sides are
+// above the minimum and even; eps = MG_EPS * 2^l.  Returns the elements of
+// the level arrays (64-element aligned level bases: TMA wants 16-byte bases).
+static size_t build_levels(int fw, int fh, uint32_t min_size, std::vector<MgLevel>& levels) {
+  levels.clear();
+  int nx = fw, ny = fh, l = 0;
+  size_t off = 0;
+  for (;;) {
+    levels.push_back(MgLevel{nx, ny, off, (float)1e-4 * (float)(1u << l)});
+    off += ((size_t)nx * ny + 63) & ~(size_t)63;
+    if ((uint32_t)nx > min_size && (uint32_t)ny > min_size && nx % 2 == 0 && ny % 2 == 0) {
+      nx /= 2;
+      ny /= 2;
+      l++;
+    } else {
+      break;
+    }
+  }
+  return off;
+}
+
+// Device bytes World::init allocates for `c` (the sum of its buffers).
+size_t world_footprint(const ribo_world_cfg& c) {
+  const size_t C = (size_t)c.grid_w * c.grid_h, F = (size_t)c.fluid_w * c.fluid_h;
+  const size_t L = (size_t)(c.grid_w / 2) * (c.grid_h / 2);
+  std::vector<MgLevel> lv;
+  const size_t M = build_levels((int)c.fluid_w, (int)c.fluid_h, c.mg_min_size ? c.mg_min_size : 8, lv);
+  size_t b = 0;
+  b += C * (16 + 16 + 4 + 8 + 4 + 4);                             // chem a/b, gamma, slope, agg_act, agg_nb
+  b += 2 * L * 4 * 2;                                             // light, shade
+  b += F * (1 + 8 + 4 + 8 * 3 + 4 * 3 + 4 * 5 + 8 * 3 + 4 + 4);  // mask..heat, mask32, p_tmp
+  b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 + MAX_STEPS * 12 * 4 + 16;
+  b += M * (4 + 4 + 1 + 4);                                       // mg p, rhs, fluid, p2
+  b += 2 * MAX_STEPS * sizeof(ribo_sim_params);
+  return b;
 }
 
 ribo_status World::init(const ribo_world_cfg& c) {
@@ -208,6 +265,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   fh = (int)cfg.fluid_h;
   ribo_world_settings_default(&st);
   RB_TRY(bind(), "device");
+  keep_pool_memory((int)cfg.device);
   RB_TRY(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "stream");
   stream = own_stream;
   size_t C = cells(), F = fcells(), L = lcells();
@@ -250,25 +308,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   redox_cur = redox_a;
   redox_nxt = redox_b;
 
-  // Multigrid levels (src/world/mod.rs:637-671): halve while both sides are
-  // above the minimum and even; eps = MG_EPS * 2^l.
-  levels.clear();
-  {
-    int nx = fw, ny = fh, l = 0;
-    size_t off = 0;
-    for (;;) {
-      levels.push_back(MgLevel{nx, ny, off, (float)1e-4 * (float)(1u << l)});
-      off += ((size_t)nx * ny + 63) & ~(size_t)63;  // 64-element aligned level bases (TMA wants 16-byte bases)
-      if ((uint32_t)nx > cfg.mg_min_size && (uint32_t)ny > cfg.mg_min_size && nx % 2 == 0 && ny % 2 == 0) {
-        nx /= 2;
-        ny /= 2;
-        l++;
-      } else {
-        break;
-      }
-    }
-    mg_total = off;
-  }
+  mg_total = build_levels(fw, fh, cfg.mg_min_size, levels);
   RB_ALLOC(mg.p, mg_total * 4);
   RB_ALLOC(mg.rhs, mg_total * 4);
   RB_ALLOC(mg.fluid, mg_total);
@@ -302,7 +342,8 @@ World::~World() {
   if (stream) cudaStreamSynchronize(stream);
   for (GraphEntry& g : graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
-  for (void* p : allocs) cudaFree(p);
+  for (void* p : allocs) cudaFreeAsync(p, own_stream);
+  if (own_stream) cudaStreamSynchronize(own_stream);
   if (h_params) cudaFreeHost(h_params);
   for (int k = 0; k < 2; k++)
     if (param_ev[k]) cudaEventDestroy(param_ev[k]);
@@ -642,9 +683,7 @@ void ribo_world_settings_default(ribo_world_settings* o) {
   o->jacobi_iters = 128;
 }
 
-ribo_status ribo_world_create(const ribo_world_cfg* cfg, ribo_world** out) {
-  if (!cfg || !out) return set_error(RIBO_INVALID_ARG, "null argument");
-  *out = nullptr;
+static ribo_status check_cfg(const ribo_world_cfg* cfg) {
   if (cfg->grid_w < 2 || cfg->grid_h < 2 || cfg->fluid_w < 2 || cfg->fluid_h < 2)
     return set_error(RIBO_INVALID_ARG, "grid and fluid sides must be >= 2");
   if (cfg->grid_w % cfg->fluid_w || cfg->grid_h % cfg->fluid_h || cfg->grid_w / cfg->fluid_w != cfg->grid_h / cfg->fluid_h)
@@ -653,6 +692,28 @@ ribo_status ribo_world_create(const ribo_world_cfg* cfg, ribo_world** out) {
   if ((uint64_t)cfg->grid_w * cfg->grid_h > (1ull << 28))
     return set_error(RIBO_INVALID_ARG, "grid too large (at most 2^28 cells: chem slot indices are u32)");
   if (cfg->precision_mode > RIBO_PRECISION_MIXED) return set_error(RIBO_INVALID_ARG, "unknown precision mode");
+  return RIBO_OK;
+}
+
+ribo_status ribo_world_footprint(const ribo_world_cfg* cfg, uint64_t* bytes) {
+  if (!cfg || !bytes) return set_error(RIBO_INVALID_ARG, "null argument");
+  ribo_status st = check_cfg(cfg);
+  if (st != RIBO_OK) return st;
+  *bytes = ribo::world_footprint(*cfg);
+  return RIBO_OK;
+}
+
+ribo_status ribo_world_memory(const ribo_world* w, uint64_t* bytes) {
+  if (!w || !bytes) return set_error(RIBO_INVALID_ARG, "null argument");
+  *bytes = w->w.device_bytes;
+  return RIBO_OK;
+}
+
+ribo_status ribo_world_create(const ribo_world_cfg* cfg, ribo_world** out) {
+  if (!cfg || !out) return set_error(RIBO_INVALID_ARG, "null argument");
+  *out = nullptr;
+  ribo_status cst = check_cfg(cfg);
+  if (cst != RIBO_OK) return cst;
   ribo_world* w = new (std::nothrow) ribo_world();
   if (!w) return set_error(RIBO_OOM, "host allocation");
   ribo_status st = w->w.init(*cfg);

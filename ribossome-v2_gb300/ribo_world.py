@@ -76,6 +76,32 @@ class KernelTiming(ctypes.Structure):
                 ("bytes", ctypes.c_double)]
 
 
+class ServerCfg(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_uint32), ("max_chunk_steps", ctypes.c_uint32), ("max_active", ctypes.c_uint32),
+                ("reserved0", ctypes.c_uint32), ("hbm_budget_bytes", ctypes.c_uint64), ("reserved", ctypes.c_uint64 * 2)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("world", WorldCfg), ("settings", WorldSettings), ("params", SimParams), ("steps", ctypes.c_uint32),
+                ("reserved0", ctypes.c_uint32), ("user_tag", ctypes.c_uint64),
+                ("inputs", ctypes.c_void_p * 16), ("outputs", ctypes.c_void_p * 16)]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("user_tag", ctypes.c_uint64), ("status", ctypes.c_int32),
+                ("steps", ctypes.c_uint32), ("ledger", ctypes.c_uint32 * 12), ("device_bytes", ctypes.c_uint64),
+                ("t_submit_ms", ctypes.c_double), ("t_admit_ms", ctypes.c_double), ("t_done_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("pending", ctypes.c_uint64), ("active", ctypes.c_uint64), ("bytes_in_use", ctypes.c_uint64),
+                ("world_steps", ctypes.c_uint64), ("iterations", ctypes.c_uint64), ("gpu_ms", ctypes.c_double)]
+
+
+assert ctypes.sizeof(Job) == 832 and ctypes.sizeof(JobResult) == 104 and ctypes.sizeof(ServerCfg) == 40
+
+
 class RiboError(RuntimeError):
     pass
 
@@ -129,6 +155,18 @@ def load_library(path: str = LIB_PATH):
         "ribo_batch_elapsed_ms": ([vp, ctypes.c_uint32, ctypes.c_uint32, P(ctypes.c_float)], ctypes.c_int),
         "ribo_batch_autotune": ([vp, P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_batch_set_tile_modes": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
+        "ribo_batch_step_ragged": ([vp, P(SimParams), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
+        "ribo_world_footprint": ([P(WorldCfg), P(ctypes.c_uint64)], ctypes.c_int),
+        "ribo_world_memory": ([vp, P(ctypes.c_uint64)], ctypes.c_int),
+        "ribo_server_create": ([P(ServerCfg), P(vp)], ctypes.c_int),
+        "ribo_server_destroy": ([vp], None),
+        "ribo_server_submit": ([vp, P(Job), P(ctypes.c_uint64)], ctypes.c_int),
+        "ribo_server_iterate": ([vp, P(ctypes.c_uint32)], ctypes.c_int),
+        "ribo_server_drain": ([vp], ctypes.c_int),
+        "ribo_server_results": ([vp, P(JobResult), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
+        "ribo_server_get_stats": ([vp, P(ServerStats)], ctypes.c_int),
+        "ribo_server_iterations": ([vp, P(ctypes.c_float), P(ctypes.c_uint32), P(ctypes.c_uint32), ctypes.c_uint32,
+                                    P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_batch_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "ribo_batch_read_kernel_timing": ([vp, P(KernelTiming), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
     }
@@ -459,3 +497,122 @@ class Batch:
         n = ctypes.c_uint32()
         check(self._lib.ribo_batch_read_kernel_timing(self._h, arr, cap, ctypes.byref(n)), "read timing")
         return [(arr[i].name.decode(), arr[i].launches, arr[i].ms, arr[i].bytes) for i in range(min(n.value, cap))]
+
+
+def world_footprint(grid, fluid=None, mg_min_size: int = 8) -> int:
+    """Device bytes a world of this configuration allocates (no GPU needed)."""
+    gw, gh = (grid, grid) if isinstance(grid, int) else grid
+    fw, fh = (gw, gh) if fluid is None else ((fluid, fluid) if isinstance(fluid, int) else fluid)
+    cfg = WorldCfg(gw, gh, fw, fh, 30, mg_min_size)
+    out = ctypes.c_uint64()
+    check(load_library().ribo_world_footprint(ctypes.byref(cfg), ctypes.byref(out)), "footprint")
+    return out.value
+
+
+class Server:
+    """World-step jobs served with continuous batching under an HBM budget."""
+
+    def __init__(self, hbm_budget_bytes: int, max_chunk_steps: int = 16, max_active: int = 0, device: int = 0):
+        lib = load_library()
+        cfg = ServerCfg(device, max_chunk_steps, max_active, 0, hbm_budget_bytes)
+        h = ctypes.c_void_p()
+        check(lib.ribo_server_create(ctypes.byref(cfg), ctypes.byref(h)), "ribo_server_create")
+        self._h = h
+        self._lib = lib
+        self.device = device
+        self._keep = {}  # job id -> (job struct, input arrays, output arrays)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ribo_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, grid, fluid=None, *, steps: int, params: SimParams, settings: WorldSettings = None,
+               inputs: dict = None, outputs=(), mg_min_size: int = 8, mg_pre: int = 2, mg_post: int = 2,
+               mg_coarse: int = 30, user_tag: int = 0) -> int:
+        """Queues a job; `outputs` lists the fields returned with its result."""
+        gw, gh = (grid, grid) if isinstance(grid, int) else grid
+        fw, fh = (gw, gh) if fluid is None else ((fluid, fluid) if isinstance(fluid, int) else fluid)
+        j = Job()
+        j.world = WorldCfg(gw, gh, fw, fh, 30, mg_min_size, mg_pre, mg_post, mg_coarse, 0, self.device, 0)
+        j.settings = settings if settings is not None else default_settings()
+        j.params = params
+        j.steps = steps
+        j.user_tag = user_tag
+        shapes = _field_shapes(gw, gh, fw, fh)
+        keep_in = []
+        for f, arr in (inputs or {}).items():
+            shape, dt = shapes[f]
+            a = np.ascontiguousarray(arr, dtype=dt).reshape(shape)
+            keep_in.append(a)
+            j.inputs[f] = a.ctypes.data
+        outs = {}
+        for f in outputs:
+            shape, dt = shapes[f]
+            outs[f] = np.zeros(shape, dtype=dt)
+            j.outputs[f] = outs[f].ctypes.data
+        jid = ctypes.c_uint64()
+        check(self._lib.ribo_server_submit(self._h, ctypes.byref(j), ctypes.byref(jid)), "ribo_server_submit")
+        self._keep[jid.value] = (j, outs)
+        return jid.value
+
+    def iterate(self) -> int:
+        a = ctypes.c_uint32()
+        check(self._lib.ribo_server_iterate(self._h, ctypes.byref(a)), "ribo_server_iterate")
+        return a.value
+
+    def drain(self):
+        check(self._lib.ribo_server_drain(self._h), "ribo_server_drain")
+
+    def results(self):
+        """[(JobResult, {field: array})] of the jobs finished since the last call."""
+        cap = 256
+        out = []
+        while True:
+            arr = (JobResult * cap)()
+            n = ctypes.c_uint32()
+            check(self._lib.ribo_server_results(self._h, arr, cap, ctypes.byref(n)), "results")
+            for i in range(n.value):
+                r = JobResult()
+                ctypes.memmove(ctypes.byref(r), ctypes.byref(arr[i]), ctypes.sizeof(JobResult))
+                _, outs = self._keep.pop(r.id, (None, {}))
+                out.append((r, outs))
+            if n.value < cap:
+                return out
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        check(self._lib.ribo_server_get_stats(self._h, ctypes.byref(s)), "stats")
+        return s
+
+    def iterations(self):
+        """[(device ms, steps, resident jobs)] per iteration since the last call."""
+        cap = 4096
+        out = []
+        while True:
+            ms = (ctypes.c_float * cap)()
+            st = (ctypes.c_uint32 * cap)()
+            ac = (ctypes.c_uint32 * cap)()
+            n = ctypes.c_uint32()
+            check(self._lib.ribo_server_iterations(self._h, ms, st, ac, cap, ctypes.byref(n)), "iterations")
+            out += [(ms[i], st[i], ac[i]) for i in range(n.value)]
+            if n.value < cap:
+                return out
+
+
+def _field_shapes(gw, gh, fw, fh):
+    C, F, L = (gh, gw), (fh, fw), (gh // 2, gw // 2)
+    return {
+        CHEM: (C + (4,), np.uint32), GAMMA: (C, np.uint32), LIGHT: ((2,) + L, np.float32),
+        SLOPE: (C + (2,), np.float32), VELOCITY: (F + (2,), np.float32), PRESSURE: (F, np.float32),
+        TEMP: (F, np.float32), REDOX: (F, np.float32), HEAT: (F + (2,), np.float32),
+        VEL_SMOOTH: (F + (2,), np.float32), SOLID_MASK: (F, np.uint32), DIVERGENCE: (F, np.float32),
+        FORCE_VECTORS: (F + (2,), np.uint32), REDOX_EATEN: (F, np.uint32),
+        NET_FLUX: ((fh + fw,), np.float32), SHADE: ((2,) + L, np.uint32),
+    }

@@ -42,8 +42,12 @@ def _lattice(seed: int, octave: int, ix: np.ndarray, iy: np.ndarray) -> np.ndarr
 
 
 def value_noise(w: int, h: int, seed: int, octaves: int = 4, base_period: float = 64.0, persistence: float = 0.5) -> np.ndarray:
-    """Fractal value noise in [0, 1], shape (h, w), float32."""
-    ys, xs = np.mgrid[0:h, 0:w].astype(np.float64)
+    """Fractal value noise in [0, 1], shape (h, w), float32.
+
+    The lattice values are hashed once per lattice point and gathered per
+    cell (the same values as hashing per cell)."""
+    xs = np.arange(w, dtype=np.float64)[None, :]
+    ys = np.arange(h, dtype=np.float64)[:, None]
     out = np.zeros((h, w))
     amp, norm, period = 1.0, 0.0, base_period
     for o in range(octaves):
@@ -52,10 +56,13 @@ def value_noise(w: int, h: int, seed: int, octaves: int = 4, base_period: float 
         tx, ty = px - ix, py - iy
         sx, sy = tx * tx * (3 - 2 * tx), ty * ty * (3 - 2 * ty)
         ix, iy = ix.astype(np.int64), iy.astype(np.int64)
-        a = _lattice(seed, o, ix, iy)
-        b = _lattice(seed, o, ix + 1, iy)
-        c = _lattice(seed, o, ix, iy + 1)
-        d = _lattice(seed, o, ix + 1, iy + 1)
+        lx = np.arange(int(ix.max()) + 2, dtype=np.int64)[None, :]
+        ly = np.arange(int(iy.max()) + 2, dtype=np.int64)[:, None]
+        lat = _lattice(seed, o, lx, ly)  # lat[j, i] = lattice value at (i, j)
+        a = lat[iy, ix]
+        b = lat[iy, ix + 1]
+        c = lat[iy + 1, ix]
+        d = lat[iy + 1, ix + 1]
         v = (a + (b - a) * sx) * (1 - sy) + (c + (d - c) * sx) * sy
         out += amp * v
         norm += amp

@@ -113,3 +113,38 @@ def test_batch_null_arguments_are_rejected(rw):
     assert lib.ribo_batch_set_tile_modes(None, None, 0) == 1
     assert lib.ribo_batch_size(None) == 0
     lib.ribo_batch_destroy(None)
+
+
+def test_world_footprint_counts_every_buffer(rw):
+    """The footprint is the sum of the world's buffers (restated here from the
+    buffer list: env cells C, fluid cells F, light cells L, multigrid M)."""
+    for (gw, gh), (fw, fh), mg in (((2048, 2048), (2048, 2048), 16), ((256, 128), (128, 64), 8), ((96, 96), (96, 96), 8)):
+        C, F, L = gw * gh, fw * fh, (gw // 2) * (gh // 2)
+        M, nx, ny = 0, fw, fh
+        while True:
+            M += (nx * ny + 63) // 64 * 64
+            if nx > mg and ny > mg and nx % 2 == 0 and ny % 2 == 0:
+                nx, ny = nx // 2, ny // 2
+            else:
+                break
+        want = C * 52 + 16 * L + F * 101 + (fw + fh) * 4 + 48 + 64 * 48 + 16 + M * 13 + 2 * 64 * 464
+        assert rw.world_footprint((gw, gh), (fw, fh), mg_min_size=mg) == want
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-GPU error path")
+def test_server_without_gpu_reports_cuda_error(rw):
+    with pytest.raises(rw.RiboError) as e:
+        rw.Server(1 << 30)
+    assert "CUDA_ERROR" in str(e.value)
+
+
+def test_server_bad_arguments(rw):
+    lib = rw.load_library()
+    h = ctypes.c_void_p()
+    cfg = rw.ServerCfg(0, 0, 0, 0, 1 << 30)  # max_chunk_steps 0
+    assert lib.ribo_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    cfg = rw.ServerCfg(0, 8, 0, 0, 0)  # zero budget
+    assert lib.ribo_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert lib.ribo_server_submit(None, None, None) == 1
+    assert lib.ribo_server_iterate(None, None) == 1
+    lib.ribo_server_destroy(None)
