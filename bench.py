@@ -24,6 +24,10 @@ transport + ledger) of one world.
   serving  (N = 1) the continuous-batching server fed by a Poisson request
          stream (200 req/s for 60 s, 150 GB budget), and again at a rate the
          GPU sustains: world-steps/s, p50/p99 step and job latency
+  mixed_precision  (N = 1) the same step with the pressure solved to a
+         relative residual of 1e-5 every step; residual re-checked in FP64
+  --ncu-case   seed the world and run --steps steps with nothing else (a
+         short program for ncu captures; prints nothing)
 N > 1 GPUs run independent replicas (one world per rank, no collective).
 """
 import argparse
@@ -373,6 +377,9 @@ def run_ours(args):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(n)
     # batched and served forms: single-GPU runs only (replicas would repeat them per rank)
+    if ws == 1 and not args.no_mixed:
+        w.close()
+        line["mixed_precision"] = run_mixed(args, local)
     if ws == 1 and not args.no_batched:
         w.close()
         line["batched"] = run_batched(args, local)
@@ -490,6 +497,50 @@ def run_batched(args, local):
         "worlds": n, "steps": steps, "cells": total_cells, "plain": plain, "batched": batched,
         "speedup": batched["world_steps_per_s"] / plain["world_steps_per_s"],
         "latency_note": "plain: one world's step alone; batched: one batched step (advances every world)",
+    }
+
+
+def run_mixed(args, local):
+    """The full-size step with the mixed-precision pressure solve: every solve
+    iterated to a relative residual of 1e-5 (FP32-pair defect correction,
+    FP32 flexible CG, FP16-storage V-cycle levels 0-3, FP64 coarsest solve and
+    per-region mean removal).  The last solve's residual is re-evaluated on the
+    host in FP64 against the operator of oracle/fp64_pressure.py."""
+    import numpy as np
+    import fp64_pressure as fp
+    import ribo_world as rw
+    import synth
+
+    n = args.size
+    w = rw.World(n, seed=1000, mg_min_size=16, mg_pre=3, mg_post=3, precision_mode=1, device=local)
+    w.seed_inputs(synth.make_world_inputs(n, seed=1000))
+    w.params = synth.bench_params(1000)
+    w.settings.fluid_substep = 1
+    warm = max(args.warmup, 3)
+    w.run(warm)
+    w.sync()
+    steps = args.mixed_steps
+    iters = []
+    w.mark(0)
+    done = 0
+    while done < steps:
+        k = min(rw.MAX_STEPS_PER_FRAME, steps - done)
+        w.encode_steps(k)
+        done += k
+    w.mark(1)
+    ms = w.elapsed_ms(0, 1)
+    for _ in range(4):  # per-solve iteration counts of a few more steps
+        w.encode_steps(1)
+        iters.append(w.solve_info())
+    water = w.read(rw.SOLID_MASK) == 0
+    p = w.read(rw.PRESSURE).astype(np.float64) + w.read(rw.PRESSURE_LO).astype(np.float64)
+    rho = fp.rel_residual(p, w.read(rw.DIVERGENCE), water)
+    w.close()
+    return {
+        "workload": f"{n}x{n} full world step, pressure solved to relative residual 1e-5 every step (mixed precision)",
+        "world_steps_per_s": steps / (ms / 1000.0), "ms_per_step": ms / steps, "steps": steps,
+        "solves": [{"outer": o, "cg_iterations": i, "rel_residual_device": r} for o, i, r in iters],
+        "rel_residual_fp64_host": rho, "tolerance": 1e-5,
     }
 
 
@@ -618,6 +669,8 @@ def main():
     ap.add_argument("--latency-samples", type=int, default=5)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed-steps", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-drain-seconds", type=float, default=0.0)
@@ -626,7 +679,22 @@ def main():
     ap.add_argument("--serve-queue", type=int, default=4)
     ap.add_argument("--serve-sustainable-rate", type=float, default=6.0)
     ap.add_argument("--serve-sustainable-seconds", type=float, default=40.0)
+    ap.add_argument("--ncu-case", action="store_true")
+    ap.add_argument("--ncu-mixed", action="store_true")
     args = ap.parse_args()
+    if args.ncu_case:
+        import ribo_world as rw
+        import synth
+
+        w = rw.World(args.size, seed=1000, mg_min_size=16, mg_pre=3, mg_post=3, no_graphs=1,
+                     precision_mode=1 if args.ncu_mixed else 0)
+        w.settings.fluid_substep = 1
+        w.settings.mg_cycles = 4
+        w.seed_inputs(synth.make_world_inputs(args.size, seed=1000))
+        w.params = synth.bench_params(1000)
+        w.run(args.steps)
+        w.sync()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -189,6 +189,13 @@ typedef struct ribo_world_settings {
   uint32_t ledger_each_step;  // 1 = run ledger_reduce after every step (read with ribo_world_step_ledgers)
   uint32_t mg_unfused;        // 1 = one dispatch per half-sweep (the reference's recording); 0 = fused kernels (same bits)
   uint32_t transport_simple;  // 1 = one thread per cell for the transport scatter; 0 = mover-parallel tiles (same bits)
+  // Mixed-precision pressure solve (precision_mode = RIBO_PRECISION_MIXED;
+  // zero fields take the defaults in brackets):
+  float mixed_tol;            // relative residual ||rhs - L p|| / ||rhs|| to reach [1e-5]
+  float mixed_inner_tol;      // residual reduction of one inner conjugate-gradient solve [1e-3]
+  uint32_t mixed_max_outer;   // defect-correction steps at most [4]
+  uint32_t mixed_max_inner;   // conjugate-gradient iterations per step at most [64]
+  float mixed_alpha;          // over-relaxation of the V-cycle's coarse correction [1.8]
 } ribo_world_settings;
 
 // Device fields a caller can upload / read.  Sizes in bytes, for a world with
@@ -211,7 +218,8 @@ typedef enum ribo_field {
   RIBO_FIELD_REDOX_EATEN = 13,   // F*4:  fixed-point reductant consumed by agents
   RIBO_FIELD_NET_FLUX = 14,      // (fluid_h+fluid_w)*4: row means of v_y then column means of v_x
   RIBO_FIELD_SHADE = 15,         // 2*L*4: agent shade per light cell (fixed point, 100 = one)
-  RIBO_FIELD_COUNT = 16,
+  RIBO_FIELD_PRESSURE_LO = 16,   // F*4:  mixed precision only: pressure = PRESSURE + PRESSURE_LO (read-only)
+  RIBO_FIELD_COUNT = 17,
 } ribo_field;
 
 // Last error text of the calling thread ("" if none).
@@ -308,6 +316,13 @@ ribo_status ribo_world_read_kernel_timing(ribo_world* w, ribo_kernel_timing* out
 
 // Number of kernels this library has launched in this process so far.
 uint64_t ribo_kernel_launch_count(void);
+
+// Mixed-precision worlds: statistics of the last pressure solve -- outer
+// defect-correction steps, conjugate-gradient iterations in total, and the
+// relative residual ||rhs - L(p_hi + p_lo)|| / ||rhs|| of the pressure it
+// left (evaluated on the device in FP32-pair arithmetic).  Waits.  No
+// counterpart in the reference.
+ribo_status ribo_world_solve_info(ribo_world* w, uint32_t* outer, uint32_t* inner, double* rel_residual);
 
 // ---- Batches: many worlds advanced together ---------------------------------
 // No single counterpart in the reference, whose World::encode_steps

@@ -1,0 +1,826 @@
+// Mixed-precision pressure solve (ribo_world_cfg.precision_mode =
+// RIBO_PRECISION_MIXED): the world step's pressure Poisson problem solved to
+// a relative residual tolerance instead of a fixed number of V-cycles.
+//
+// The problem is the reference's level-0 operator (shaders/world/
+// multigrid.wgsl:29-77) written exactly: for every water cell,
+//     (L p)_i = sum over water neighbours j of (p_j - p_i) - eps0 * p_i,
+// eps0 = 1e-4 (the f32 value), and L p = rhs with rhs = the divergence.
+//
+// * Outer loop (defect correction): the solution is kept as an unevaluated
+//   pair of FP32 numbers (pressure_a = hi, a second buffer = lo); the
+//   residual rhs - L(hi + lo) is evaluated with error-free FP32
+//   transformations (Knuth's TwoSum, Dekker's FastTwoSum, the FMA two-product),
+//   which resolves it to ~2^-44 where a single FP32 vector stalls at ~1e-5
+//   relative residual on 256^2 and above.
+// * Inner loop: flexible conjugate gradients in FP32 on L e = r
+//   (Polak-Ribiere beta, which tolerates the preconditioner's FP16 rounding),
+//   preconditioned by a symmetric V-cycle: FP16 storage of the smoothing
+//   arrays on levels 0-3, FP32 below, an exact FP64 solve on the coarsest
+//   level (dense inverse), and FP64 mean removal: every connected water
+//   region is a pure-Neumann-like problem whose constant vector is an exact
+//   eigenvector of L (eigenvalue -eps0), so the preconditioner removes the
+//   residual's mean per region before the V-cycle and adds the exact
+//   constant correction -mean/eps0 after it.
+// * Both loops run on the device as CUDA graph WHILE nodes; their bodies'
+//   last kernels decide whether to iterate again, with hard caps on the
+//   iteration counts.  No host synchronisation happens inside a solve.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stddef.h>
+#include <string.h>
+
+#include <vector>
+
+#include "ribo_dev.cuh"
+#include "ribo_launch.h"
+#include "ribo_world_impl.h"
+
+namespace ribo {
+
+namespace {
+
+constexpr int BX = PASS_BX, BY = PASS_BY, NT = BX * BY;
+constexpr int COMP_CAP = 65536;        // water components tracked (later ones share the last slot)
+constexpr int COARSEST_CAP = 1024;     // cells of the coarsest level (dense FP64 inverse)
+constexpr int HALF_LEVELS = 4;         // fine levels 0..3 store FP16
+
+// ---- FP32 pair ("double-float") arithmetic -------------------------------
+struct df32 {
+  float hi, lo;
+};
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ df32 two_sum(float a, float b) {
+  const float s = a + b;
+  const float bp = s - a;
+  const float e = (a - (s - bp)) + (b - bp);
+  return df32{s, e};
+}
+// Dekker's FastTwoSum (|a| >= |b|).
+__device__ __forceinline__ df32 fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return df32{s, b - (s - a)};
+}
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+  df32 s = two_sum(a.hi, b.hi);
+  const df32 t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = fast_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df32 df_neg(df32 a) { return df32{-a.hi, -a.lo}; }
+// (hi + lo) * b with the FMA two-product of hi * b.
+__device__ __forceinline__ df32 df_mul_f(df32 a, float b) {
+  const float p = a.hi * b;
+  float e = __fmaf_rn(a.hi, b, -p);
+  e += a.lo * b;
+  return fast_two_sum(p, e);
+}
+
+// ---- solver state --------------------------------------------------------
+struct MpCtl {
+  unsigned int done;  // blocks finished in the current reduction kernel
+  int outer, inner, total_inner;
+  int converged, inner_done;
+  int max_outer, max_inner;
+  int ncomp;
+  float tol2, itol2;  // squared relative tolerances
+  float rz, alpha, beta;
+  float scale[2];     // V-cycle input scale and its inverse
+  float r0n2;         // ||r||^2 at the start of the outer iteration
+  float itarget2;     // squared residual reduction the inner solve stops at
+  float nwater;
+  double bn2;         // ||rhs||^2
+  double rho;         // relative residual of the last outer evaluation
+};
+
+struct MpArgs {
+  int fw, fh;
+  float eps0;
+  float* hi;  // pressure_a
+  float* lo;
+  const float* rhs;     // divergence
+  const uint8_t* fl;    // level-0 water flags
+  const int* label;     // component per cell (-1: wall)
+  float *r, *e, *d, *q, *z;
+  float* part;          // per-block partial sums [blocks][2]
+  MpCtl* ctl;
+  double* comp_sum_r;
+  double* comp_sum_z;
+  double* comp_mean;
+  const double* comp_size;
+};
+
+struct Cell {
+  int x, y;
+  size_t i;
+  bool in, water;
+};
+__device__ __forceinline__ Cell cell_of(const MpArgs& a) {
+  Cell c;
+  c.x = blockIdx.x * BX + threadIdx.x;
+  c.y = blockIdx.y * BY + threadIdx.y;
+  c.in = c.x < a.fw && c.y < a.fh;
+  c.i = c.in ? (size_t)c.y * a.fw + c.x : 0;
+  c.water = c.in && a.fl[c.i] != 0;
+  return c;
+}
+
+// Block sums of two values written to the per-block partials; returns true in
+// every thread of the block that finished last (its partials are visible).
+__device__ __forceinline__ bool block_partials(const MpArgs& a, float v0, float v1) {
+  __shared__ float s0[NT / 32], s1[NT / 32];
+  __shared__ bool last;
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  for (int o = 16; o > 0; o >>= 1) {
+    v0 += __shfl_down_sync(0xffffffffu, v0, o);
+    v1 += __shfl_down_sync(0xffffffffu, v1, o);
+  }
+  if ((tid & 31) == 0) {
+    s0[tid >> 5] = v0;
+    s1[tid >> 5] = v1;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float t0 = 0.0f, t1 = 0.0f;
+    for (int w = 0; w < NT / 32; w++) {
+      t0 += s0[w];
+      t1 += s1[w];
+    }
+    const unsigned b = blockIdx.y * gridDim.x + blockIdx.x;
+    a.part[2 * b] = t0;
+    a.part[2 * b + 1] = t1;
+    __threadfence();
+    const unsigned n = gridDim.x * gridDim.y;
+    last = atomicAdd(&a.ctl->done, 1u) == n - 1;
+  }
+  __syncthreads();
+  return last;
+}
+
+// In the last block: the totals of the partials, summed in a fixed order
+// (deterministic), returned in every thread.
+__device__ __forceinline__ void total_partials(const MpArgs& a, float& t0, float& t1) {
+  __shared__ float s0[NT], s1[NT];
+  __threadfence();
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  const unsigned n = gridDim.x * gridDim.y;
+  float v0 = 0.0f, v1 = 0.0f;
+  for (unsigned b = tid; b < n; b += NT) {
+    v0 += ((volatile float*)a.part)[2 * b];
+    v1 += ((volatile float*)a.part)[2 * b + 1];
+  }
+  s0[tid] = v0;
+  s1[tid] = v1;
+  __syncthreads();
+  for (int o = NT / 2; o > 0; o >>= 1) {
+    if (tid < o) {
+      s0[tid] += s0[tid + o];
+      s1[tid] += s1[tid + o];
+    }
+    __syncthreads();
+  }
+  t0 = s0[0];
+  t1 = s1[0];
+  __syncthreads();
+}
+
+// Per-component FP64 sums of a per-cell value (block-aggregated for the
+// block's first water component).
+__device__ __forceinline__ void comp_add(const MpArgs& a, double* sums, const Cell& c, double v) {
+  __shared__ int dom;
+  __shared__ double sh[NT / 32];
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  if (tid == 0) {
+    int dm = -1;
+    for (int j = 0; j < BY && dm < 0; j++)
+      for (int i = 0; i < BX && dm < 0; i++) {
+        const int x = blockIdx.x * BX + i, y = blockIdx.y * BY + j;
+        if (x < a.fw && y < a.fh) dm = a.label[(size_t)y * a.fw + x];
+      }
+    dom = dm;
+  }
+  __syncthreads();
+  double own = 0.0;
+  if (c.water) {
+    const int lab = a.label[c.i];
+    if (lab == dom) own = v;
+    else atomicAdd(sums + lab, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) own += __shfl_down_sync(0xffffffffu, own, o);
+  if ((tid & 31) == 0) sh[tid >> 5] = own;
+  __syncthreads();
+  if (tid == 0 && dom >= 0) {
+    double t = 0.0;
+    for (int w = 0; w < NT / 32; w++) t += sh[w];
+    atomicAdd(sums + dom, t);
+  }
+  __threadfence();  // the sums are complete before this block counts itself done
+}
+
+// In the last block: component means of the residual (FP64) and the power-of-
+// two scale that brings its RMS to ~1 for the FP16 levels.
+__device__ __forceinline__ void finish_residual_stats(const MpArgs& a, float rn2) {
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  MpCtl* ctl = a.ctl;
+  const int nc = ctl->ncomp;
+  for (int c = tid; c < nc; c += NT) {
+    a.comp_mean[c] = a.comp_size[c] > 0.0 ? __ldcg(a.comp_sum_r + c) / a.comp_size[c] : 0.0;
+    a.comp_sum_r[c] = 0.0;
+  }
+  if (tid == 0) {
+    const float rms = ctl->nwater > 0.0f ? sqrtf(rn2 / ctl->nwater) : 0.0f;
+    float sc = 1.0f;
+    if (rms > 0.0f && rms == rms) {
+      int ex = 0;
+      frexpf(rms, &ex);
+      sc = ldexpf(1.0f, -ex);
+    }
+    ctl->scale[0] = sc;
+    ctl->scale[1] = 1.0f / sc;
+  }
+}
+
+__global__ void k_mp_begin(MpArgs a, int max_outer, int max_inner, float tol, float itol,
+                           cudaGraphConditionalHandle h_outer) {
+  MpCtl* ctl = a.ctl;
+  for (int c = threadIdx.x; c < ctl->ncomp; c += blockDim.x) {
+    a.comp_sum_r[c] = 0.0;
+    a.comp_sum_z[c] = 0.0;
+  }
+  if (threadIdx.x == 0) {
+    ctl->done = 0;
+    ctl->outer = ctl->inner = ctl->total_inner = 0;
+    ctl->converged = ctl->inner_done = 0;
+    ctl->max_outer = max_outer;
+    ctl->max_inner = max_inner;
+    ctl->tol2 = tol * tol;
+    ctl->itol2 = itol * itol;
+    ctl->bn2 = 0.0;
+    ctl->rho = 0.0;
+    cudaGraphSetConditional(h_outer, 1u);
+  }
+}
+
+// Outer residual r = rhs - L(hi + lo) in FP32-pair arithmetic; the CG
+// starts from e = 0 on it.  The last block decides both loops.
+__global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphConditionalHandle h_outer,
+                                                    cudaGraphConditionalHandle h_inner, int final_pass) {
+  const Cell c = cell_of(a);
+  float rf = 0.0f, b = 0.0f;
+  if (c.water) {
+    const df32 pi = df32{a.hi[c.i], a.lo[c.i]};
+    df32 s = df32{0.0f, 0.0f};
+    const int nb[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int x = c.x + nb[k][0], y = c.y + nb[k][1];
+      if (x < 0 || y < 0 || x >= a.fw || y >= a.fh) continue;
+      const size_t j = (size_t)y * a.fw + x;
+      if (!a.fl[j]) continue;
+      s = df_add(s, df_add(df32{a.hi[j], a.lo[j]}, df_neg(pi)));
+    }
+    const df32 lp = df_add(s, df_neg(df_mul_f(pi, a.eps0)));
+    b = a.rhs[c.i];
+    const df32 res = df_add(df32{b, 0.0f}, df_neg(lp));
+    rf = res.hi + res.lo;
+  }
+  if (c.in) {
+    a.r[c.i] = rf;
+    a.e[c.i] = 0.0f;
+  }
+  comp_add(a, a.comp_sum_r, c, (double)rf);
+  if (!block_partials(a, rf * rf, b * b)) return;
+  float rn2, bn2;
+  total_partials(a, rn2, bn2);
+  MpCtl* ctl = a.ctl;
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  if (final_pass) {
+    for (int k = tid; k < ctl->ncomp; k += NT) a.comp_sum_r[k] = 0.0;
+    if (tid == 0) {
+      ctl->rho = ctl->bn2 > 0.0 ? sqrt((double)rn2 / ctl->bn2) : 0.0;
+      ctl->done = 0;
+    }
+    return;
+  }
+  finish_residual_stats(a, rn2);
+  if (tid == 0) {
+    if (ctl->outer == 0) ctl->bn2 = (double)bn2;
+    const double rho2 = ctl->bn2 > 0.0 ? (double)rn2 / ctl->bn2 : 0.0;
+    ctl->rho = sqrt(rho2);
+    const bool conv = rho2 <= (double)ctl->tol2 || !(rho2 == rho2);
+    ctl->converged = conv ? 1 : 0;
+    ctl->inner = 0;
+    ctl->inner_done = conv ? 1 : 0;
+    ctl->r0n2 = rn2;
+    // the inner solve stops at mixed_inner_tol, or as soon as the outer
+    // residual would be half the tolerance if it is closer than that
+    const double need = rho2 > 0.0 ? 0.25 * (double)ctl->tol2 / rho2 : 1.0;
+    ctl->itarget2 = (float)(need > (double)ctl->itol2 ? (need < 1.0 ? need : 1.0) : (double)ctl->itol2);
+    ctl->outer += 1;
+    ctl->done = 0;
+    cudaGraphSetConditional(h_inner, conv ? 0u : 1u);
+    cudaGraphSetConditional(h_outer, (!conv && ctl->outer < ctl->max_outer) ? 1u : 0u);
+  }
+}
+
+// z <- z - (mean of z over its component) - comp_mean / eps0, then the dot
+// products z.r and z.q of the flexible CG.
+__global__ void __launch_bounds__(NT) k_mp_dots(MpArgs a) {
+  const Cell c = cell_of(a);
+  float zr = 0.0f, zq = 0.0f;
+  if (c.water) {
+    const int lab = a.label[c.i];
+    const double zm = a.comp_size[lab] > 0.0 ? a.comp_sum_z[lab] / a.comp_size[lab] : 0.0;
+    const float zc = (float)((double)a.z[c.i] - zm - a.comp_mean[lab] / (double)a.eps0);
+    a.z[c.i] = zc;
+    zr = zc * a.r[c.i];
+    zq = zc * a.q[c.i];
+  } else if (c.in) {
+    a.z[c.i] = 0.0f;
+  }
+  if (!block_partials(a, zr, zq)) return;
+  float tzr, tzq;
+  total_partials(a, tzr, tzq);
+  MpCtl* ctl = a.ctl;
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  for (int k = tid; k < ctl->ncomp; k += NT) a.comp_sum_z[k] = 0.0;
+  if (tid == 0) {
+    ctl->beta = (ctl->inner == 0 || ctl->rz == 0.0f) ? 0.0f : -ctl->alpha * tzq / ctl->rz;
+    ctl->rz = tzr;
+    ctl->done = 0;
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_mp_direction(MpArgs a) {
+  const Cell c = cell_of(a);
+  if (!c.in) return;
+  const float beta = a.ctl->beta;
+  const bool first = a.ctl->inner == 0;  // d starts as z (whatever d held before)
+  a.d[c.i] = c.water ? (first ? a.z[c.i] : a.z[c.i] + beta * a.d[c.i]) : 0.0f;
+}
+
+// q = L d in FP32 (differences first, so a constant d gives -eps0 * d
+// exactly), and d.q; alpha = z.r / d.q.
+__global__ void __launch_bounds__(NT) k_mp_matvec(MpArgs a) {
+  const Cell c = cell_of(a);
+  float dq = 0.0f;
+  if (c.water) {
+    const float di = a.d[c.i];
+    float s = 0.0f;
+    if (c.x > 0 && a.fl[c.i - 1]) s += a.d[c.i - 1] - di;
+    if (c.x + 1 < a.fw && a.fl[c.i + 1]) s += a.d[c.i + 1] - di;
+    if (c.y > 0 && a.fl[c.i - a.fw]) s += a.d[c.i - a.fw] - di;
+    if (c.y + 1 < a.fh && a.fl[c.i + a.fw]) s += a.d[c.i + a.fw] - di;
+    const float q = s - a.eps0 * di;
+    a.q[c.i] = q;
+    dq = di * q;
+  } else if (c.in) {
+    a.q[c.i] = 0.0f;
+  }
+  if (!block_partials(a, dq, 0.0f)) return;
+  float tdq, unused;
+  total_partials(a, tdq, unused);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    MpCtl* ctl = a.ctl;
+    ctl->alpha = tdq != 0.0f ? ctl->rz / tdq : 0.0f;
+    ctl->done = 0;
+  }
+}
+
+// e += alpha d, r -= alpha q; the last block tests the inner tolerance,
+// prepares the next preconditioner input and sets the inner loop condition.
+__global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHandle h_inner) {
+  const Cell c = cell_of(a);
+  const float alpha = a.ctl->alpha;
+  float rn = 0.0f;
+  if (c.water) {
+    a.e[c.i] += alpha * a.d[c.i];
+    rn = a.r[c.i] - alpha * a.q[c.i];
+    a.r[c.i] = rn;
+  }
+  comp_add(a, a.comp_sum_r, c, (double)rn);
+  if (!block_partials(a, rn * rn, 0.0f)) return;
+  float rn2, unused;
+  total_partials(a, rn2, unused);
+  finish_residual_stats(a, rn2);
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  if (tid == 0) {
+    MpCtl* ctl = a.ctl;
+    ctl->inner += 1;
+    ctl->total_inner += 1;
+    const bool done = rn2 <= ctl->itarget2 * ctl->r0n2 || !(rn2 == rn2);
+    ctl->inner_done = done ? 1 : 0;
+    ctl->done = 0;
+    cudaGraphSetConditional(h_inner, (!done && ctl->inner < ctl->max_inner) ? 1u : 0u);
+  }
+}
+
+// (hi, lo) += e; walls hold 0 (as the f32 multigrid leaves them).
+__global__ void __launch_bounds__(NT) k_mp_update(MpArgs a) {
+  const Cell c = cell_of(a);
+  if (!c.in) return;
+  if (!c.water) {
+    a.hi[c.i] = 0.0f;
+    a.lo[c.i] = 0.0f;
+    return;
+  }
+  const df32 p = df_add(df32{a.hi[c.i], a.lo[c.i]}, df32{a.e[c.i], 0.0f});
+  a.hi[c.i] = p.hi;
+  a.lo[c.i] = p.lo;
+}
+
+}  // namespace
+
+// Buffers and graphs of one world's mixed-precision solver.
+struct MixedSolver {
+  float* lo = nullptr;
+  float *r = nullptr, *e = nullptr, *d = nullptr, *q = nullptr, *z = nullptr;
+  float* part = nullptr;
+  int* label = nullptr;
+  MpCtl* ctl = nullptr;
+  double *comp_sum_r = nullptr, *comp_sum_z = nullptr, *comp_mean = nullptr, *comp_size = nullptr;
+  double* inv = nullptr;
+  int coarsest_cells = 0;
+  MpHierarchy h{};
+  cudaStream_t cap[3] = {nullptr, nullptr, nullptr};
+  cudaGraphExec_t standalone = nullptr;
+  ribo_world_settings built_for{};
+  int ncomp = 0;
+};
+
+namespace {
+
+int half_levels(const World& w) {
+  const int k = multigrid_first_coarse_level(w.levels.data(), (int)w.levels.size());
+  return k < HALF_LEVELS ? k : HALF_LEVELS;
+}
+
+MpArgs mp_args(const World& w, const MixedSolver& m) {
+  MpArgs a{};
+  a.fw = w.fw;
+  a.fh = w.fh;
+  a.eps0 = (float)1e-4;
+  a.hi = w.pa;
+  a.lo = m.lo;
+  a.rhs = w.div;
+  a.fl = w.mg.fluid + w.levels[0].off;
+  a.label = m.label;
+  a.r = m.r;
+  a.e = m.e;
+  a.d = m.d;
+  a.q = m.q;
+  a.z = m.z;
+  a.part = m.part;
+  a.ctl = m.ctl;
+  a.comp_sum_r = m.comp_sum_r;
+  a.comp_sum_z = m.comp_sum_z;
+  a.comp_mean = m.comp_mean;
+  a.comp_size = m.comp_size;
+  return a;
+}
+
+float setting_or(float v, float dflt) { return v > 0.0f ? v : dflt; }
+int setting_or(uint32_t v, int dflt) { return v > 0 ? (int)v : dflt; }
+
+#define RB_CK(expr)                       \
+  do {                                    \
+    cudaError_t _e = (expr);              \
+    if (_e != cudaSuccess) return _e;     \
+  } while (0)
+
+// Adds the solve to the graph that stream `s` is capturing: a WHILE node for
+// the outer loop whose body holds the residual, a WHILE node for the inner
+// loop and the update.
+cudaError_t capture_solve(World& w, MixedSolver& m, cudaStream_t s) {
+  const MpArgs a = mp_args(w, m);
+  const dim3 grid((w.fw + BX - 1) / BX, (w.fh + BY - 1) / BY), blk(BX, BY);
+  const ribo_world_settings& st = w.st;
+  cudaStreamCaptureStatus cs;
+  unsigned long long id = 0;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* ed = nullptr;
+  size_t nd = 0;
+  RB_CK(cudaStreamGetCaptureInfo(s, &cs, &id, &g, &deps, &ed, &nd));
+  if (cs != cudaStreamCaptureStatusActive) return cudaErrorIllegalState;
+  // Each handle belongs to the graph that contains its WHILE node; neither has
+  // a default value: a kernel sets it before its node runs (k_mp_begin for the
+  // outer loop, k_mp_residual for the inner one), and the bodies' last kernels
+  // stop the loops once converged or at the iteration caps.
+  cudaGraphConditionalHandle ho, hi;
+  RB_CK(cudaGraphConditionalHandleCreate(&ho, g, 0, 0));
+  k_mp_begin<<<1, 256, 0, s>>>(a, setting_or(st.mixed_max_outer, 4), setting_or(st.mixed_max_inner, 64),
+                               setting_or(st.mixed_tol, 1e-5f), setting_or(st.mixed_inner_tol, 1e-3f), ho);
+  RB_CK(cudaGetLastError());
+  RB_CK(cudaStreamGetCaptureInfo(s, &cs, &id, &g, &deps, &ed, &nd));
+  cudaGraphNodeParams po = {};
+  po.type = cudaGraphNodeTypeConditional;
+  po.conditional.handle = ho;
+  po.conditional.type = cudaGraphCondTypeWhile;
+  po.conditional.size = 1;
+  cudaGraphNode_t no;
+  RB_CK(cudaGraphAddNode(&no, g, deps, ed, nd, &po));
+  cudaGraph_t body_o = po.conditional.phGraph_out[0];
+  RB_CK(cudaStreamUpdateCaptureDependencies(s, &no, nullptr, 1, cudaStreamSetCaptureDependencies));
+
+  RB_CK(cudaGraphConditionalHandleCreate(&hi, body_o, 0, 0));
+
+  // outer body: residual, inner loop, update
+  cudaStream_t so = m.cap[1];
+  RB_CK(cudaStreamBeginCaptureToGraph(so, body_o, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  k_mp_residual<<<grid, blk, 0, so>>>(a, ho, hi, 0);
+  cudaGraph_t gb = nullptr;
+  RB_CK(cudaStreamGetCaptureInfo(so, &cs, &id, &gb, &deps, &ed, &nd));
+  cudaGraphNodeParams pi = {};
+  pi.type = cudaGraphNodeTypeConditional;
+  pi.conditional.handle = hi;
+  pi.conditional.type = cudaGraphCondTypeWhile;
+  pi.conditional.size = 1;
+  cudaGraphNode_t ni;
+  RB_CK(cudaGraphAddNode(&ni, gb, deps, ed, nd, &pi));
+  cudaGraph_t body_i = pi.conditional.phGraph_out[0];
+  RB_CK(cudaStreamUpdateCaptureDependencies(so, &ni, nullptr, 1, cudaStreamSetCaptureDependencies));
+  k_mp_update<<<grid, blk, 0, so>>>(a);
+  cudaGraph_t tmp = nullptr;
+  RB_CK(cudaStreamEndCapture(so, &tmp));
+
+  // inner body: one flexible-CG iteration
+  cudaStream_t si = m.cap[2];
+  RB_CK(cudaStreamBeginCaptureToGraph(si, body_i, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  MpHierarchy h = m.h;
+  h.alpha = setting_or(st.mixed_alpha, 1.8f);
+  h.pre = (int)w.cfg.mg_pre;
+  h.post = (int)w.cfg.mg_post;
+  launch_mixed_vcycle(w.dev(), w.levels.data(), (int)w.levels.size(), w.mg, h, si);
+  k_mp_dots<<<grid, blk, 0, si>>>(a);
+  k_mp_direction<<<grid, blk, 0, si>>>(a);
+  k_mp_matvec<<<grid, blk, 0, si>>>(a);
+  k_mp_axpy<<<grid, blk, 0, si>>>(a, hi);
+  RB_CK(cudaStreamEndCapture(si, &tmp));
+
+  k_mp_residual<<<grid, blk, 0, s>>>(a, ho, hi, 1);  // residual of the result
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Allocates the solver's buffers (World::init of a mixed-precision world).
+ribo_status mixed_init(World& w) {
+  const int nl = (int)w.levels.size();
+  const int k = multigrid_first_coarse_level(w.levels.data(), nl);
+  const MgLevel& last = w.levels[nl - 1];
+  if (k == 0)
+    return set_error(RIBO_INVALID_ARG, "mixed precision needs a fluid grid above %d cells", 4096);
+  if ((long)last.nx * last.ny > COARSEST_CAP)
+    return set_error(RIBO_INVALID_ARG, "mixed precision: coarsest level %dx%d above %d cells (raise mg_min_size)", last.nx,
+                     last.ny, COARSEST_CAP);
+  MixedSolver* m = new (std::nothrow) MixedSolver;
+  if (!m) return set_error(RIBO_OOM, "host allocation");
+  w.mixed = m;
+  const size_t F = w.fcells();
+  const size_t blocks = ((size_t)(w.fw + BX - 1) / BX) * ((w.fh + BY - 1) / BY);
+  ribo_status r;
+#define MP_ALLOC(ptr, bytes) \
+  if ((r = w.alloc((void**)&(ptr), (bytes), #ptr)) != RIBO_OK) return r;
+  MP_ALLOC(m->lo, F * 4);
+  MP_ALLOC(m->r, F * 4);
+  MP_ALLOC(m->e, F * 4);
+  MP_ALLOC(m->d, F * 4);
+  MP_ALLOC(m->q, F * 4);
+  MP_ALLOC(m->z, F * 4);
+  MP_ALLOC(m->label, F * 4);
+  MP_ALLOC(m->part, blocks * 2 * 4);
+  MP_ALLOC(m->ctl, sizeof(MpCtl));
+  MP_ALLOC(m->comp_sum_r, COMP_CAP * 8);
+  MP_ALLOC(m->comp_sum_z, COMP_CAP * 8);
+  MP_ALLOC(m->comp_mean, COMP_CAP * 8);
+  MP_ALLOC(m->comp_size, COMP_CAP * 8);
+  m->coarsest_cells = last.nx * last.ny;
+  MP_ALLOC(m->inv, (size_t)m->coarsest_cells * m->coarsest_cells * 8);
+  const int nh = half_levels(w);
+  m->h.nhalf = nh;
+  for (int l = 0; l < k; l++) {
+    const size_t n = (size_t)w.levels[l].nx * w.levels[l].ny;
+    const size_t es = l < nh ? 2 : 4;
+    MP_ALLOC(m->h.fine[l].ef, n * es);
+    if (l > 0) {
+      MP_ALLOC(m->h.fine[l].rhs, n * es);
+      MP_ALLOC(m->h.fine[l].E, n * 4);
+    }
+  }
+#undef MP_ALLOC
+  m->h.r = m->r;
+  m->h.label = m->label;
+  m->h.comp_mean = m->comp_mean;
+  m->h.scale = reinterpret_cast<const float*>(reinterpret_cast<const char*>(m->ctl) + offsetof(MpCtl, scale));
+  m->h.z = m->z;
+  m->h.comp_sum_z = m->comp_sum_z;
+  m->h.coarse_inv = m->inv;
+  for (int i = 0; i < 3; i++)
+    if (cudaStreamCreateWithFlags(&m->cap[i], cudaStreamNonBlocking) != cudaSuccess)
+      return cuda_status(cudaGetLastError(), "stream");
+  multigrid_prepare_mixed();
+  return RIBO_OK;
+}
+
+// Device bytes mixed_init adds for a world with these levels.
+size_t mixed_footprint(const ribo_world_cfg& c, const std::vector<MgLevel>& levels) {
+  const size_t F = (size_t)c.fluid_w * c.fluid_h;
+  const size_t blocks = ((size_t)(c.fluid_w + BX - 1) / BX) * ((c.fluid_h + BY - 1) / BY);
+  const int nl = (int)levels.size();
+  const int k = multigrid_first_coarse_level(levels.data(), nl);
+  const size_t nc = (size_t)levels[nl - 1].nx * levels[nl - 1].ny;
+  size_t b = F * 4 * 7 + blocks * 8 + sizeof(MpCtl) + (size_t)COMP_CAP * 8 * 4 + nc * nc * 8;
+  const int nh = k < HALF_LEVELS ? k : HALF_LEVELS;
+  for (int l = 0; l < k; l++) {
+    const size_t n = (size_t)levels[l].nx * levels[l].ny, es = l < nh ? 2 : 4;
+    b += n * es + (l > 0 ? n * es + n * 4 : 0);
+  }
+  return b;
+}
+
+void mixed_free(World& w) {
+  MixedSolver* m = w.mixed;
+  if (!m) return;
+  if (m->standalone) cudaGraphExecDestroy(m->standalone);
+  for (int i = 0; i < 3; i++)
+    if (m->cap[i]) cudaStreamDestroy(m->cap[i]);
+  delete m;
+  w.mixed = nullptr;
+}
+
+// Dense inverse by Gauss-Jordan elimination with partial pivoting (FP64).
+static bool invert(std::vector<double>& a, int n, std::vector<double>& inv) {
+  inv.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) inv[(size_t)i * n + i] = 1.0;
+  for (int col = 0; col < n; col++) {
+    int piv = col;
+    for (int r = col + 1; r < n; r++)
+      if (fabs(a[(size_t)r * n + col]) > fabs(a[(size_t)piv * n + col])) piv = r;
+    if (a[(size_t)piv * n + col] == 0.0) return false;
+    if (piv != col)
+      for (int j = 0; j < n; j++) {
+        std::swap(a[(size_t)piv * n + j], a[(size_t)col * n + j]);
+        std::swap(inv[(size_t)piv * n + j], inv[(size_t)col * n + j]);
+      }
+    const double p = a[(size_t)col * n + col];
+    for (int j = 0; j < n; j++) {
+      a[(size_t)col * n + j] /= p;
+      inv[(size_t)col * n + j] /= p;
+    }
+    for (int r = 0; r < n; r++) {
+      if (r == col) continue;
+      const double f = a[(size_t)r * n + col];
+      if (f == 0.0) continue;
+      for (int j = 0; j < n; j++) {
+        a[(size_t)r * n + j] -= f * a[(size_t)col * n + j];
+        inv[(size_t)r * n + j] -= f * inv[(size_t)col * n + j];
+      }
+    }
+  }
+  return true;
+}
+
+// After every wall-mask build: water components (labels, sizes), the water
+// flags of every level (any water child), and the dense inverse of the
+// coarsest level's operator.  Runs on the host from the mask read back.
+ribo_status mixed_setup(World& w) {
+  MixedSolver* m = w.mixed;
+  if (!m) return RIBO_OK;
+  const int fw = w.fw, fh = w.fh;
+  const size_t F = w.fcells();
+  std::vector<uint8_t> mask(F);
+  cudaError_t e = cudaMemcpyAsync(mask.data(), w.mask, F, cudaMemcpyDeviceToHost, w.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w.stream);
+  if (e != cudaSuccess) return cuda_status(e, "mixed setup");
+  // 4-connected water components (breadth-first)
+  std::vector<int> label(F, -1);
+  std::vector<double> size(COMP_CAP, 0.0);
+  std::vector<int> queue;
+  queue.reserve(F);
+  int ncomp = 0;
+  for (size_t s = 0; s < F; s++) {
+    if (mask[s] || label[s] >= 0) continue;
+    const int id = ncomp < COMP_CAP ? ncomp : COMP_CAP - 1;
+    ncomp++;
+    queue.clear();
+    queue.push_back((int)s);
+    label[s] = id;
+    for (size_t qi = 0; qi < queue.size(); qi++) {
+      const int i = queue[qi], x = i % fw, y = i / fw;
+      size[id] += 1.0;
+      const int nb[4] = {x > 0 ? i - 1 : -1, x + 1 < fw ? i + 1 : -1, y > 0 ? i - fw : -1, y + 1 < fh ? i + fw : -1};
+      for (int j : nb)
+        if (j >= 0 && !mask[j] && label[j] < 0) {
+          label[j] = id;
+          queue.push_back(j);
+        }
+    }
+  }
+  if (ncomp > COMP_CAP) ncomp = COMP_CAP;
+  m->ncomp = ncomp;
+  // level water flags
+  const int nl = (int)w.levels.size();
+  std::vector<std::vector<uint8_t>> fl(nl);
+  fl[0].resize(F);
+  for (size_t i = 0; i < F; i++) fl[0][i] = mask[i] ? 0 : 1;
+  for (int l = 1; l < nl; l++) {
+    const int nx = w.levels[l].nx, ny = w.levels[l].ny, px = w.levels[l - 1].nx;
+    fl[l].assign((size_t)nx * ny, 0);
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        const size_t c0 = (size_t)(2 * y) * px + 2 * x;
+        fl[l][(size_t)y * nx + x] = (fl[l - 1][c0] | fl[l - 1][c0 + 1] | fl[l - 1][c0 + px] | fl[l - 1][c0 + px + 1]) ? 1 : 0;
+      }
+  }
+  // coarsest operator: sum over water neighbours - (k + eps) on water cells, identity on the others
+  const MgLevel& cl = w.levels[nl - 1];
+  const int n = cl.nx * cl.ny;
+  std::vector<double> A((size_t)n * n, 0.0), inv;
+  const std::vector<uint8_t>& cf = fl[nl - 1];
+  for (int y = 0; y < cl.ny; y++)
+    for (int x = 0; x < cl.nx; x++) {
+      const int i = y * cl.nx + x;
+      if (!cf[i]) {
+        A[(size_t)i * n + i] = 1.0;
+        continue;
+      }
+      int k = 0;
+      const int nb[4] = {x > 0 ? i - 1 : -1, x + 1 < cl.nx ? i + 1 : -1, y > 0 ? i - cl.nx : -1,
+                         y + 1 < cl.ny ? i + cl.nx : -1};
+      for (int j : nb)
+        if (j >= 0 && cf[j]) {
+          A[(size_t)i * n + j] = 1.0;
+          k++;
+        }
+      A[(size_t)i * n + i] = -((double)k + (double)cl.eps);
+    }
+  if (!invert(A, n, inv)) return set_error(RIBO_CUDA_ERROR, "mixed setup: singular coarsest operator");
+  // upload
+  e = cudaMemcpyAsync(m->label, label.data(), F * 4, cudaMemcpyHostToDevice, w.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->comp_size, size.data(), COMP_CAP * 8, cudaMemcpyHostToDevice, w.stream);
+  for (int l = 1; l < nl && e == cudaSuccess; l++)
+    e = cudaMemcpyAsync(w.mg.fluid + w.levels[l].off, fl[l].data(), fl[l].size(), cudaMemcpyHostToDevice, w.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->inv, inv.data(), inv.size() * 8, cudaMemcpyHostToDevice, w.stream);
+  MpCtl ctl{};
+  ctl.ncomp = ncomp;
+  double nwater = 0.0;
+  for (int c = 0; c < ncomp; c++) nwater += size[c];
+  ctl.nwater = (float)nwater;
+  ctl.scale[0] = ctl.scale[1] = 1.0f;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->ctl, &ctl, sizeof ctl, cudaMemcpyHostToDevice, w.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w.stream);
+  return cuda_status(e, "mixed setup");
+}
+
+// The pressure solve of one step, on the world's stream.  Inside a step
+// capture the solve's loops become nodes of the captured graph; otherwise a
+// standalone graph of the solve (built once per settings) is launched.
+ribo_status mixed_solve(World& w) {
+  MixedSolver* m = w.mixed;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(w.stream, &cs);
+  if (e != cudaSuccess) return cuda_status(e, "mixed solve");
+  if (cs == cudaStreamCaptureStatusActive) {
+    e = capture_solve(w, *m, w.stream);
+    return cuda_status(e, "mixed solve capture");
+  }
+  if (m->standalone && memcmp(&m->built_for, &w.st, sizeof w.st) != 0) {
+    cudaGraphExecDestroy(m->standalone);
+    m->standalone = nullptr;
+  }
+  if (!m->standalone) {
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(m->cap[0], cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaError_t ce = capture_solve(w, *m, m->cap[0]);
+      e = cudaStreamEndCapture(m->cap[0], &g);
+      if (ce != cudaSuccess) e = ce;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&m->standalone, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_status(e, "mixed solve graph");
+    m->built_for = w.st;
+  }
+  RB_LAUNCH("mixed_pressure_solve", 0.0, w.stream, e = cudaGraphLaunch(m->standalone, w.stream));
+  return cuda_status(e, "mixed solve launch");
+}
+
+ribo_status mixed_info(World& w, uint32_t* outer, uint32_t* inner, double* rho) {
+  if (!w.mixed) return set_error(RIBO_INVALID_ARG, "the world is not in mixed-precision mode");
+  MpCtl c{};
+  cudaError_t e = cudaMemcpyAsync(&c, w.mixed->ctl, sizeof c, cudaMemcpyDeviceToHost, w.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w.stream);
+  if (e != cudaSuccess) return cuda_status(e, "mixed info");
+  if (outer) *outer = (uint32_t)c.outer;
+  if (inner) *inner = (uint32_t)c.total_inner;
+  if (rho) *rho = c.rho;
+  return RIBO_OK;
+}
+
+float* mixed_pressure_lo(World& w) { return w.mixed ? w.mixed->lo : nullptr; }
+
+}  // namespace ribo

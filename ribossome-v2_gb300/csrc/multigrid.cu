@@ -6,6 +6,7 @@
 // Red-black sweeps update one colour from the other colour only, so every
 // fused or tiled variant below produces the same bits as one dispatch per
 // half-sweep.
+#include <cuda_fp16.h>
 #include <string.h>
 
 #include <vector>
@@ -273,14 +274,15 @@ __device__ __forceinline__ bool box_load(uint32_t* status, const Lv& L, const fl
 }
 
 // Half-sweeps 0..nsweeps-1 on the box; sweep s updates the cells at distance
-// >= s+1 from the edge of the valid region (multigrid.wgsl:60-77).
+// >= s+1 from the edge of the valid region (multigrid.wgsl:60-77).  Colour
+// (x + y) & 1 of sweep s is (s & 1) ^ c0: red first for c0 = 0.
 template <int TW, int TH>
 __device__ __forceinline__ void box_sweeps(int nsweeps, int H, int RH, int bx, int by, float eps, float* sp, const float* sr,
-                                           const uint8_t* sf) {
+                                           const uint8_t* sf, int c0 = 0) {
   constexpr int BOXW = TW + 2 * BOXX;
   const int ilo = BOXX - H, ihi = BOXX + TW + H;
   for (int s = 0; s < nsweeps; s++) {
-    const int color = s & 1;
+    const int color = (s & 1) ^ c0;
     const int m = s + 1;
     for (int j = m + threadIdx.y; j < RH - m; j += BY) {
       const int gy = by + j;
@@ -404,6 +406,13 @@ struct CoarsePass {
   float* pa;
   int fw;
   int top;
+  // Mixed-precision preconditioner form (null inv: the reference's V-cycle):
+  // restriction 1/2 * sum over water children, the coarse correction
+  // prolonged times `alpha`, post-smoothing colours reversed (the V-cycle is
+  // then a symmetric operator), and the coarsest level solved exactly in
+  // FP64 with its dense inverse `inv` (row-major, cells x cells).
+  const double* inv;
+  float alpha;
 };
 struct CoarseOne {
   CoarsePass e;
@@ -435,7 +444,7 @@ __device__ __forceinline__ void sm_sweep(int nx, int ny, float eps, float* p, co
   __syncthreads();
 }
 
-template <class S>
+template <class S, bool MP = false>
 __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ S s, int nu_pre, int nu_post, int coarse) {
   const CoarsePass& e = coarse_of(s);
   const CoarseSet& cs = e.cs;
@@ -497,12 +506,27 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
         nf++;
       }
       fc[cidx] = nf > 0u ? 1 : 0;
-      rc[cidx] = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
+      if (MP) rc[cidx] = nf > 0u ? 0.5f * sum : 0.0f;
+      else rc[cidx] = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
       pc[cidx] = 0.0f;
     }
     __syncthreads();
   }
-  {
+  if (MP) {
+    // exact coarsest solve in FP64: one warp per row of the dense inverse
+    const int l = cs.n - 1, nc = cs.nx[l] * cs.ny[l];
+    const float* rc = R + cs.off[l];
+    float* pcst = P + cs.off[l];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = warp; i < nc; i += COARSE_THREADS / 32) {
+      const double* row = e.inv + (size_t)i * nc;
+      double acc = 0.0;
+      for (int j = lane; j < nc; j += 32) acc += row[j] * (double)rc[j];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (lane == 0) pcst[i] = (float)acc;
+    }
+    __syncthreads();
+  } else {
     const int l = cs.n - 1;
     for (int k = 0; k < coarse; k++) {
       sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], P + cs.off[l], R + cs.off[l], F + cs.off[l], 0u);
@@ -519,12 +543,13 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
     for (int y = ty; y < cs.ny[l]; y += rows)
       for (int x = tx; x < nx; x += 32) {
         const int idx = y * nx + x;
-        if (f[idx]) p[idx] += pc[(y / 2) * cnx + x / 2];
+        if (f[idx]) p[idx] += MP ? e.alpha * pc[(y / 2) * cnx + x / 2] : pc[(y / 2) * cnx + x / 2];
       }
     __syncthreads();
+    const uint32_t c0 = MP ? 1u : 0u;
     for (int k = 0; k < nu_post; k++) {
-      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, 0u);
-      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, 1u);
+      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, c0);
+      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, c0 ^ 1u);
     }
   }
   {
@@ -661,6 +686,7 @@ static void set_smem_attrs() {
   set_tile_attrs<32, 16>(mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseMany>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mg_coarse<CoarseOne, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   attr_done |= 1ull << (dev & 63);
 }
 
@@ -943,6 +969,295 @@ void launch_multigrid_batch_pre(const MgBatchPlan* plan, int level, cudaStream_t
   set_smem_attrs();
   for (const MgBatchPlan::Group& g : plan->groups)
     if (g.level == level) launch_group_pre(g, plan->c, s);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision preconditioner V-cycle (the solver around it is in
+// mixed.cu).
+//
+// It approximates L e = r for the scaled, component-mean-free residual r of
+// the flexible CG.  A fine level keeps two arrays of type T (FP16 on the
+// first levels, FP32 below): its right-hand side and its pre-smoothed
+// correction e_f.  Post-smoothing adds the coarse level's total correction
+// (FP32, times alpha) to e_f in shared memory and sweeps in FP32, so the
+// large smooth part of a correction is never rounded to FP16; a level's
+// total correction leaves as FP32 (levels >= 1) or, on level 0, as the
+// unscaled output z with its per-component sums (FP64).  Restriction is
+// 1/2 * sum over the water children (the transpose of the piecewise-constant
+// prolongation up to the factor that keeps R L P the coarse operator), and
+// post-smoothing runs the colours in reverse order, so the V-cycle is a
+// symmetric operator.  Every level loads with plain loads.
+namespace {
+
+struct MpLevelArgs {
+  int nx, ny;
+  float eps;
+  const uint8_t* fl;  // water flags of the level
+  const void* rhs;    // right-hand side (type T); level 0: the CG residual (float)
+  void* ef;           // pre-smoothed correction (type T)
+  int cnx, cny;
+  void* crhs;         // coarse right-hand side (pre output)
+  const float* cE;    // coarse total correction (post input)
+  float* E;           // total correction of the level (post output, levels >= 1)
+  float alpha;
+  // level 0
+  const int* label;          // water component of each cell (-1: wall)
+  const double* comp_mean;   // mean of the CG residual per component
+  const float* scale;        // [0] scale applied to the residual, [1] its inverse
+  float* z;                  // V-cycle output, unscaled
+  double* comp_sum_z;        // per-component sums of z
+};
+
+__device__ __forceinline__ float mp_ld(const float* p, size_t i) { return p[i]; }
+__device__ __forceinline__ float mp_ld(const __half* p, size_t i) { return __half2float(p[i]); }
+__device__ __forceinline__ void mp_st(float* p, size_t i, float v) { p[i] = v; }
+__device__ __forceinline__ void mp_st(__half* p, size_t i, float v) { p[i] = __float2half_rn(v); }
+
+// The level's right-hand side at a water cell; level 0 removes the
+// component mean (FP64) and applies the FP16 scale.
+template <bool TOP, class T>
+__device__ __forceinline__ float mp_rhs(const MpLevelArgs& a, size_t gi, float sc) {
+  if (TOP) {
+    const double r = (double)static_cast<const float*>(a.rhs)[gi];
+    return (float)((r - a.comp_mean[a.label[gi]]) * (double)sc);
+  }
+  return mp_ld(static_cast<const T*>(a.rhs), gi);
+}
+
+template <int TW, int TH, bool TOP, class T>
+__device__ __forceinline__ void mp_load(const MpLevelArgs& a, int bx, int by, int RH, bool post, float* sp, float* sr,
+                                        uint8_t* sf) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  const int n = BOXW * RH, tid = threadIdx.y * BX + threadIdx.x;
+  const float sc = TOP ? a.scale[0] : 1.0f;
+  for (int e = tid; e < n; e += BX * BY) {
+    const int gx = bx + e % BOXW, gy = by + e / BOXW;
+    float p = 0.0f, r = 0.0f;
+    uint8_t f = 0;
+    if (gx >= 0 && gy >= 0 && gx < a.nx && gy < a.ny) {
+      const size_t gi = (size_t)gy * a.nx + gx;
+      f = a.fl[gi];
+      if (f) {
+        r = mp_rhs<TOP, T>(a, gi, sc);
+        if (post) p = mp_ld(static_cast<const T*>(a.ef), gi) + a.alpha * a.cE[(size_t)(gy / 2) * a.cnx + gx / 2];
+      }
+    }
+    sp[e] = p;
+    sr[e] = r;
+    sf[e] = f;
+  }
+  __syncthreads();
+}
+
+// Pre-smooth from zero + residual + restriction (1/2 * sum over water children).
+template <int TW, int TH, bool TOP, class T, class CT>
+__global__ void __launch_bounds__(BX* BY) k_mp_pre(const __grid_constant__ MpLevelArgs a, int nu) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int H = 2 * nu + 1, RH = TH + 2 * H;
+  float* sp = reinterpret_cast<float*>(smem_raw);
+  float* sr = sp + BOXW * RH;
+  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, bx = x0 - BOXX, by = y0 - H;
+  mp_load<TW, TH, TOP, T>(a, bx, by, RH, false, sp, sr, sf);
+  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, a.eps, sp, sr, sf, 0);
+  T* ef = static_cast<T*>(a.ef);
+  for (int j = threadIdx.y; j < TH; j += BY)
+    for (int i = threadIdx.x; i < TW; i += BX) {
+      const int gx = x0 + i, gy = y0 + j;
+      if (gx < a.nx && gy < a.ny) mp_st(ef, (size_t)gy * a.nx + gx, sp[(j + H) * BOXW + i + BOXX]);
+    }
+  CT* crhs = static_cast<CT*>(a.crhs);
+  for (int cj = threadIdx.y; cj < TH / 2; cj += BY)
+    for (int ci = threadIdx.x; ci < TW / 2; ci += BX) {
+      const int cgx = blockIdx.x * (TW / 2) + ci, cgy = blockIdx.y * (TH / 2) + cj;
+      if (cgx >= a.cnx || cgy >= a.cny) continue;
+      float sum = 0.0f;
+      uint32_t nf = 0;
+#pragma unroll
+      for (uint32_t q = 0; q < 4; q++) {
+        const int c = (H + 2 * cj + (int)(q >> 1)) * BOXW + BOXX + 2 * ci + (int)(q & 1u);
+        if (!sf[c]) continue;
+        float s = 0.0f, k = 0.0f;
+        if (sf[c - 1]) { s += sp[c - 1]; k += 1.0f; }
+        if (sf[c + 1]) { s += sp[c + 1]; k += 1.0f; }
+        if (sf[c - BOXW]) { s += sp[c - BOXW]; k += 1.0f; }
+        if (sf[c + BOXW]) { s += sp[c + BOXW]; k += 1.0f; }
+        sum += sr[c] - (s - (k + a.eps) * sp[c]);
+        nf++;
+      }
+      mp_st(crhs, (size_t)cgy * a.cnx + cgx, nf > 0u ? 0.5f * sum : 0.0f);
+    }
+}
+
+// Per-block sums of a per-cell value into per-component FP64 accumulators:
+// the block's dominant component (that of its first water cell) is summed in
+// shared memory and added once; cells of other components add directly.
+__device__ __forceinline__ void comp_accumulate(double* comp_sum, int dom, int lab, double v, double* sh) {
+  double own = 0.0;
+  if (lab >= 0) {
+    if (lab == dom) own = v;
+    else atomicAdd(comp_sum + lab, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) own += __shfl_down_sync(0xffffffffu, own, o);
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nw = (blockDim.x * blockDim.y) >> 5;
+  if ((tid & 31) == 0) sh[tid >> 5] = own;
+  __syncthreads();
+  if (tid == 0 && dom >= 0) {
+    double t = 0.0;
+    for (int w = 0; w < nw; w++) t += sh[w];
+    atomicAdd(comp_sum + dom, t);
+  }
+}
+
+// Prolong (alpha * coarse total) + post-smooth (colours reversed).
+template <int TW, int TH, bool TOP, class T>
+__global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLevelArgs a, int nu) {
+  constexpr int BOXW = TW + 2 * BOXX;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ double zsh[BX * BY / 32];
+  __shared__ int dom;
+  const int H = 2 * nu, RH = TH + 2 * H;
+  float* sp = reinterpret_cast<float*>(smem_raw);
+  float* sr = sp + BOXW * RH;
+  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, bx = x0 - BOXX, by = y0 - H;
+  mp_load<TW, TH, TOP, T>(a, bx, by, RH, true, sp, sr, sf);
+  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, a.eps, sp, sr, sf, 1);
+  if (!TOP) {
+    for (int j = threadIdx.y; j < TH; j += BY)
+      for (int i = threadIdx.x; i < TW; i += BX) {
+        const int gx = x0 + i, gy = y0 + j;
+        if (gx < a.nx && gy < a.ny) a.E[(size_t)gy * a.nx + gx] = sp[(j + H) * BOXW + i + BOXX];
+      }
+    return;
+  }
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    int d = -1;
+    for (int j = 0; j < TH && d < 0; j++)
+      for (int i = 0; i < TW && d < 0; i++) {
+        const int gx = x0 + i, gy = y0 + j;
+        if (gx < a.nx && gy < a.ny) d = a.label[(size_t)gy * a.nx + gx];
+      }
+    dom = d;
+  }
+  __syncthreads();
+  const float inv = a.scale[1];
+  double own = 0.0;
+  for (int j = threadIdx.y; j < TH; j += BY)
+    for (int i = threadIdx.x; i < TW; i += BX) {
+      const int gx = x0 + i, gy = y0 + j;
+      if (gx >= a.nx || gy >= a.ny) continue;
+      const size_t gi = (size_t)gy * a.nx + gx;
+      const int lab = a.label[gi];
+      const float z = lab >= 0 ? sp[(j + H) * BOXW + i + BOXX] * inv : 0.0f;
+      a.z[gi] = z;
+      if (lab >= 0) {
+        if (lab == dom) own += (double)z;
+        else atomicAdd(a.comp_sum_z + lab, (double)z);
+      }
+    }
+  comp_accumulate(a.comp_sum_z, dom, dom, own, zsh);
+}
+
+template <int TW, int TH>
+void mp_attrs(int mx) {
+  cudaFuncSetAttribute(k_mp_pre<TW, TH, true, __half, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_pre<TW, TH, true, __half, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_pre<TW, TH, false, __half, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_pre<TW, TH, false, __half, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_pre<TW, TH, false, float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_pre<TW, TH, true, float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_post<TW, TH, true, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_post<TW, TH, true, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_post<TW, TH, false, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_mp_post<TW, TH, false, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+template <int TW, int TH>
+void mp_launch_pre(const MpLevelArgs& a, bool top, bool half, bool chalf, int nu, cudaStream_t s) {
+  const dim3 grid((a.nx + TW - 1) / TW, (a.ny + TH - 1) / TH), blk(BX, BY);
+  const size_t sm = box_smem<TW, TH>(2 * nu + 1);
+  if (top && half && chalf) k_mp_pre<TW, TH, true, __half, __half><<<grid, blk, sm, s>>>(a, nu);
+  else if (top && half) k_mp_pre<TW, TH, true, __half, float><<<grid, blk, sm, s>>>(a, nu);
+  else if (top) k_mp_pre<TW, TH, true, float, float><<<grid, blk, sm, s>>>(a, nu);
+  else if (half && chalf) k_mp_pre<TW, TH, false, __half, __half><<<grid, blk, sm, s>>>(a, nu);
+  else if (half) k_mp_pre<TW, TH, false, __half, float><<<grid, blk, sm, s>>>(a, nu);
+  else k_mp_pre<TW, TH, false, float, float><<<grid, blk, sm, s>>>(a, nu);
+}
+
+template <int TW, int TH>
+void mp_launch_post(const MpLevelArgs& a, bool top, bool half, int nu, cudaStream_t s) {
+  const dim3 grid((a.nx + TW - 1) / TW, (a.ny + TH - 1) / TH), blk(BX, BY);
+  const size_t sm = box_smem<TW, TH>(2 * nu);
+  if (top && half) k_mp_post<TW, TH, true, __half><<<grid, blk, sm, s>>>(a, nu);
+  else if (top) k_mp_post<TW, TH, true, float><<<grid, blk, sm, s>>>(a, nu);
+  else if (half) k_mp_post<TW, TH, false, __half><<<grid, blk, sm, s>>>(a, nu);
+  else k_mp_post<TW, TH, false, float><<<grid, blk, sm, s>>>(a, nu);
+}
+
+}  // namespace
+
+void multigrid_prepare_mixed() {
+  static uint64_t attr_done = 0;  // one bit per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!(attr_done >> (dev & 63) & 1ull)) {
+    mp_attrs<64, 32>(200 * 1024);
+    mp_attrs<32, 16>(200 * 1024);
+    attr_done |= 1ull << (dev & 63);
+  }
+  set_smem_attrs();
+}
+
+int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MpHierarchy& h,
+                        cudaStream_t s) {
+  multigrid_prepare_mixed();
+  const int k = multigrid_first_coarse_level(levels, nl);
+  int launches = 0;
+  auto args = [&](int l) {
+    MpLevelArgs a{};
+    a.nx = levels[l].nx;
+    a.ny = levels[l].ny;
+    a.eps = levels[l].eps;
+    a.fl = b.fluid + levels[l].off;
+    a.rhs = l == 0 ? static_cast<const void*>(h.r) : h.fine[l].rhs;
+    a.ef = h.fine[l].ef;
+    a.cnx = levels[l + 1].nx;
+    a.cny = levels[l + 1].ny;
+    a.crhs = l + 1 < k ? h.fine[l + 1].rhs : static_cast<void*>(b.rhs + levels[k].off);
+    a.cE = l + 1 < k ? h.fine[l + 1].E : b.p + levels[k].off;
+    a.E = h.fine[l].E;
+    a.alpha = h.alpha;
+    a.label = h.label;
+    a.comp_mean = h.comp_mean;
+    a.scale = h.scale;
+    a.z = h.z;
+    a.comp_sum_z = h.comp_sum_z;
+    return a;
+  };
+  for (int l = 0; l < k; l++) {
+    const MpLevelArgs a = args(l);
+    const bool half = l < h.nhalf, chalf = l + 1 < k && l + 1 < h.nhalf;
+    if (small_tiles(levels[l])) mp_launch_pre<32, 16>(a, l == 0, half, chalf, h.pre, s);
+    else mp_launch_pre<64, 32>(a, l == 0, half, chalf, h.pre, s);
+    launches++;
+  }
+  size_t coarse_smem = 0;
+  double coarse_bytes = 0.0;
+  CoarseOne co{coarse_pass(d, levels, nl, b, &coarse_smem, &coarse_bytes)};
+  co.e.inv = h.coarse_inv;
+  co.e.alpha = h.alpha;
+  k_mg_coarse<CoarseOne, true><<<1, COARSE_THREADS, coarse_smem, s>>>(co, h.pre, h.post, 0);
+  launches++;
+  for (int l = k - 1; l >= 0; l--) {
+    const MpLevelArgs a = args(l);
+    const bool half = l < h.nhalf;
+    if (small_tiles(levels[l])) mp_launch_post<32, 16>(a, l == 0, half, h.post, s);
+    else mp_launch_post<64, 32>(a, l == 0, half, h.post, s);
+    launches++;
+  }
+  return launches;
 }
 
 }  // namespace ribo

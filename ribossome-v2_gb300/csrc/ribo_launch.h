@@ -149,6 +149,33 @@ void launch_multigrid_batch(const MgBatchPlan* plan, cudaStream_t s);
 // time tile shapes.
 void launch_multigrid_batch_pre(const MgBatchPlan* plan, int level, cudaStream_t s);
 
+// Buffers of the mixed-precision preconditioner V-cycle (owned by the world;
+// see mixed.cu).  Fine level l (below the first coarse level) stores its
+// right-hand side (l >= 1) and pre-smoothed correction as FP16 when
+// l < nhalf, else FP32, and its total correction E (l >= 1) as FP32.
+struct MpHierarchy {
+  int nhalf;
+  struct Fine {
+    void* ef;
+    void* rhs;
+    float* E;
+  } fine[16];
+  const float* r;            // level-0 input: the CG residual
+  const int* label;          // water component per fluid cell (-1: wall)
+  const double* comp_mean;   // mean residual per component
+  const float* scale;        // [0] scale, [1] inverse scale
+  float* z;                  // level-0 output
+  double* comp_sum_z;        // per-component sums of z (accumulated)
+  const double* coarse_inv;  // dense FP64 inverse of the coarsest operator
+  float alpha;               // coarse-correction over-relaxation
+  int pre, post;
+};
+// Sets the kernel attributes of the mixed V-cycle (call before capturing it).
+void multigrid_prepare_mixed();
+// Launches one V-cycle of the preconditioner; returns the launches made.
+int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nlevels, const MgBufs& b, const MpHierarchy& h,
+                        cudaStream_t s);
+
 // transport.cu
 void launch_slope(const Dev& d, float world_units_per_cell, cudaStream_t s);
 void launch_thermal(const Target& t, cudaStream_t s);

@@ -33,6 +33,17 @@ size_t world_footprint(const ribo_world_cfg& c);
 // Bytes of field `f` of a world with configuration `c` (0: no such field).
 size_t field_bytes_of(const ribo_world_cfg& c, ribo_field f);
 
+struct World;
+struct MixedSolver;
+// Mixed-precision pressure solver of a world (mixed.cu).
+ribo_status mixed_init(World& w);
+ribo_status mixed_setup(World& w);
+ribo_status mixed_solve(World& w);
+ribo_status mixed_info(World& w, uint32_t* outer, uint32_t* inner, double* rho);
+void mixed_free(World& w);
+float* mixed_pressure_lo(World& w);
+size_t mixed_footprint(const ribo_world_cfg& c, const std::vector<MgLevel>& levels);
+
 uint64_t ktime_launch_count();
 void ktime_add_launches(uint64_t n);
 // Makes `t` (cleared) the timer of the following launches on this thread, or none.
@@ -87,6 +98,8 @@ struct World {
   std::vector<MgLevel> levels;
   size_t mg_total = 0;
   size_t device_bytes = 0;  // sum of the world's device buffers
+  MixedSolver* mixed = nullptr;      // precision_mode = RIBO_PRECISION_MIXED
+  ribo_status solve_error = RIBO_OK;  // a pressure solve that failed to record
   MgBufs mg{};
   std::vector<MgLevelMaps> mg_maps;
   uint32_t* status = nullptr;  // kernel error bits (RIBO_ERR_*)

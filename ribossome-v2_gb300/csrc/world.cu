@@ -116,6 +116,7 @@ size_t field_bytes_of(const ribo_world_cfg& c, ribo_field f) {
     case RIBO_FIELD_REDOX_EATEN: return F * 4;
     case RIBO_FIELD_NET_FLUX: return (fw + fh) * 4;
     case RIBO_FIELD_SHADE: return 2 * L * 4;
+    case RIBO_FIELD_PRESSURE_LO: return F * 4;
     default: return 0;
   }
 }
@@ -138,6 +139,7 @@ void* World::field_ptr(ribo_field f) {
     case RIBO_FIELD_REDOX_EATEN: return redox_eaten;
     case RIBO_FIELD_NET_FLUX: return net_flux;
     case RIBO_FIELD_SHADE: return shade;
+    case RIBO_FIELD_PRESSURE_LO: return mixed_pressure_lo(*this);
     default: return nullptr;
   }
 }
@@ -249,6 +251,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 + MAX_STEPS * 12 * 4 + 16;
   b += M * (4 + 4 + 1 + 4);                                       // mg p, rhs, fluid, p2
   b += 2 * MAX_STEPS * sizeof(ribo_sim_params);
+  if (c.precision_mode == RIBO_PRECISION_MIXED) b += mixed_footprint(c, lv);
   return b;
 }
 
@@ -322,6 +325,12 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_TRY(cudaEventCreate(&t0), "event");
   RB_TRY(cudaEventCreate(&t1), "event");
   for (int k = 0; k < 8; k++) RB_TRY(cudaEventCreate(&marks[k]), "event");
+  if (cfg.precision_mode == RIBO_PRECISION_MIXED) {
+    const MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, 1};
+    if (!multigrid_fused_ok(levels.data(), (int)levels.size(), c))
+      return set_error(RIBO_INVALID_ARG, "mixed precision needs 1 <= mg_pre, mg_post <= 7 and a coarse level of <= 4096 cells");
+    if ((r = mixed_init(*this)) != RIBO_OK) return r;
+  }
   // gamma = 0 at creation: derive slope and mask once.
   Dev d = dev();
   {
@@ -335,11 +344,12 @@ ribo_status World::init(const ribo_world_cfg& c) {
   launch_solid_mask(target_one(d, nullptr), stream);
   RB_TRY(cudaGetLastError(), "init kernels");
   RB_TRY(cudaStreamSynchronize(stream), "init");
-  return RIBO_OK;
+  return mixed_setup(*this);
 }
 
 World::~World() {
   if (stream) cudaStreamSynchronize(stream);
+  mixed_free(*this);
   for (GraphEntry& g : graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
   for (void* p : allocs) cudaFreeAsync(p, own_stream);
@@ -362,7 +372,8 @@ ribo_status World::upload(ribo_field f, const void* host, size_t bytes) {
   if (bytes != need) return set_error(RIBO_INVALID_ARG, "field %d: %zu bytes given, %zu expected", (int)f, bytes, need);
   if (!host) return set_error(RIBO_INVALID_ARG, "null host pointer");
   RB_TRY(bind(), "device");
-  if (f == RIBO_FIELD_SOLID_MASK || f == RIBO_FIELD_SLOPE || f == RIBO_FIELD_NET_FLUX || f == RIBO_FIELD_VEL_SMOOTH)
+  if (f == RIBO_FIELD_SOLID_MASK || f == RIBO_FIELD_SLOPE || f == RIBO_FIELD_NET_FLUX || f == RIBO_FIELD_VEL_SMOOTH ||
+      f == RIBO_FIELD_PRESSURE_LO)
     return set_error(RIBO_INVALID_ARG, "field %d is derived and read-only", (int)f);
   RB_TRY(cudaMemcpyAsync(field_ptr(f), host, bytes, cudaMemcpyHostToDevice, stream), "upload");
   if (f == RIBO_FIELD_GAMMA) {
@@ -370,6 +381,8 @@ ribo_status World::upload(ribo_field f, const void* host, size_t bytes) {
     launch_slope(d, (float)cfg.world_units_per_cell, stream);
     launch_solid_mask(target_one(d, nullptr), stream);
     RB_TRY(cudaGetLastError(), "slope/mask");
+    ribo_status ms = mixed_setup(*this);
+    if (ms != RIBO_OK) return ms;
   }
   RB_TRY(cudaStreamSynchronize(stream), "upload");
   return RIBO_OK;
@@ -389,6 +402,7 @@ ribo_status World::read(ribo_field f, void* host, size_t bytes) {
   if (!host) return set_error(RIBO_INVALID_ARG, "null host pointer");
   RB_TRY(bind(), "device");
   const void* src = field_ptr(f);
+  if (!src && f != RIBO_FIELD_SOLID_MASK) return set_error(RIBO_INVALID_ARG, "field %d does not exist in this world", (int)f);
   if (f == RIBO_FIELD_SOLID_MASK) {
     size_t n = fcells();
     k_mask_to_u32<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(mask, mask32, n);
@@ -406,6 +420,11 @@ ribo_status World::read(ribo_field f, void* host, size_t bytes) {
 
 // One pressure solve, result in pressure_a (src/world/mod.rs:1545-1581).
 void World::pressure_solve(const Dev& d) {
+  if (mixed) {
+    ribo_status s = mixed_solve(*this);
+    if (s != RIBO_OK && solve_error == RIBO_OK) solve_error = s;
+    return;
+  }
   if (st.multigrid) {
     MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, (int)(st.mg_cycles < 1 ? 1 : st.mg_cycles)};
     if (!st.mg_unfused && multigrid_fused_ok(levels.data(), (int)levels.size(), c))
@@ -485,6 +504,11 @@ ribo_status World::step(const ribo_sim_params* per_step, uint32_t n) {
     if (s != RIBO_OK) return s;
   }
   last_steps = n;
+  if (solve_error != RIBO_OK) {
+    ribo_status s = solve_error;
+    solve_error = RIBO_OK;
+    return s;
+  }
   RB_TRY(cudaGetLastError(), "step launch");
   RB_TRY(cudaEventRecord(t1, stream), "event");
   return RIBO_OK;
@@ -681,6 +705,18 @@ void ribo_world_settings_default(ribo_world_settings* o) {
   o->multigrid = 1;
   o->mg_cycles = 1;
   o->jacobi_iters = 128;
+  o->mixed_tol = 1e-5f;
+  o->mixed_inner_tol = 1e-3f;
+  o->mixed_max_outer = 4;
+  o->mixed_max_inner = 64;
+  o->mixed_alpha = 1.8f;
+}
+
+ribo_status ribo_world_solve_info(ribo_world* w, uint32_t* outer, uint32_t* inner, double* rel_residual) {
+  if (!w) return set_error(RIBO_INVALID_ARG, "null world");
+  ribo_status st = ribo::cuda_status(w->w.bind(), "device");
+  if (st != RIBO_OK) return st;
+  return ribo::mixed_info(w->w, outer, inner, rel_residual);
 }
 
 static ribo_status check_cfg(const ribo_world_cfg* cfg) {

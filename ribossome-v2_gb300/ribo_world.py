@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libribo_world.so")
 # ribo_field
 CHEM, GAMMA, LIGHT, SLOPE, VELOCITY, PRESSURE, TEMP, REDOX, HEAT = range(9)
 VEL_SMOOTH, SOLID_MASK, DIVERGENCE, FORCE_VECTORS, REDOX_EATEN, NET_FLUX, SHADE = range(9, 16)
+PRESSURE_LO = 16
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "OVER_BUDGET", 4: "TIMEOUT", 5: "CUDA_ERROR"}
 MAX_STEPS_PER_FRAME = 64
@@ -68,6 +69,8 @@ class WorldSettings(ctypes.Structure):
         ("multigrid", ctypes.c_uint32), ("mg_cycles", ctypes.c_uint32),
         ("jacobi_iters", ctypes.c_uint32), ("ledger_each_step", ctypes.c_uint32),
         ("mg_unfused", ctypes.c_uint32), ("transport_simple", ctypes.c_uint32),
+        ("mixed_tol", ctypes.c_float), ("mixed_inner_tol", ctypes.c_float),
+        ("mixed_max_outer", ctypes.c_uint32), ("mixed_max_inner", ctypes.c_uint32), ("mixed_alpha", ctypes.c_float),
     ]
 
 
@@ -84,7 +87,7 @@ class ServerCfg(ctypes.Structure):
 class Job(ctypes.Structure):
     _fields_ = [("world", WorldCfg), ("settings", WorldSettings), ("params", SimParams), ("steps", ctypes.c_uint32),
                 ("reserved0", ctypes.c_uint32), ("user_tag", ctypes.c_uint64),
-                ("inputs", ctypes.c_void_p * 16), ("outputs", ctypes.c_void_p * 16)]
+                ("inputs", ctypes.c_void_p * 17), ("outputs", ctypes.c_void_p * 17)]
 
 
 class JobResult(ctypes.Structure):
@@ -99,7 +102,8 @@ class ServerStats(ctypes.Structure):
                 ("world_steps", ctypes.c_uint64), ("iterations", ctypes.c_uint64), ("gpu_ms", ctypes.c_double)]
 
 
-assert ctypes.sizeof(Job) == 832 and ctypes.sizeof(JobResult) == 104 and ctypes.sizeof(ServerCfg) == 40
+assert ctypes.sizeof(WorldSettings) == 52 and ctypes.sizeof(Job) == 872 and ctypes.sizeof(JobResult) == 104
+assert ctypes.sizeof(ServerCfg) == 40
 
 
 class RiboError(RuntimeError):
@@ -157,6 +161,7 @@ def load_library(path: str = LIB_PATH):
         "ribo_batch_set_tile_modes": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
         "ribo_batch_step_ragged": ([vp, P(SimParams), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_world_footprint": ([P(WorldCfg), P(ctypes.c_uint64)], ctypes.c_int),
+        "ribo_world_solve_info": ([vp, P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_double)], ctypes.c_int),
         "ribo_world_memory": ([vp, P(ctypes.c_uint64)], ctypes.c_int),
         "ribo_server_create": ([P(ServerCfg), P(vp)], ctypes.c_int),
         "ribo_server_destroy": ([vp], None),
@@ -290,7 +295,7 @@ class World:
             TEMP: (F, np.float32), REDOX: (F, np.float32), HEAT: (F + (2,), np.float32),
             VEL_SMOOTH: (F + (2,), np.float32), SOLID_MASK: (F, np.uint32), DIVERGENCE: (F, np.float32),
             FORCE_VECTORS: (F + (2,), np.uint32), REDOX_EATEN: (F, np.uint32),
-            NET_FLUX: ((self.fh + self.fw,), np.float32), SHADE: ((2,) + L, np.uint32),
+            NET_FLUX: ((self.fh + self.fw,), np.float32), SHADE: ((2,) + L, np.uint32), PRESSURE_LO: (F, np.float32),
         }[field]
 
     # ---- data movement ----
@@ -373,6 +378,12 @@ class World:
         ms = ctypes.c_float()
         check(self._lib.ribo_world_elapsed_ms(self._h, a, b, ctypes.byref(ms)), "elapsed")
         return ms.value
+
+    def solve_info(self):
+        """(outer steps, CG iterations, relative residual) of the last mixed-precision solve."""
+        o, i, r = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
+        check(self._lib.ribo_world_solve_info(self._h, ctypes.byref(o), ctypes.byref(i), ctypes.byref(r)), "solve_info")
+        return o.value, i.value, r.value
 
     def ledger_blocking(self) -> Ledger:
         out = (ctypes.c_uint32 * 12)()
@@ -614,5 +625,5 @@ def _field_shapes(gw, gh, fw, fh):
         TEMP: (F, np.float32), REDOX: (F, np.float32), HEAT: (F + (2,), np.float32),
         VEL_SMOOTH: (F + (2,), np.float32), SOLID_MASK: (F, np.uint32), DIVERGENCE: (F, np.float32),
         FORCE_VECTORS: (F + (2,), np.uint32), REDOX_EATEN: (F, np.uint32),
-        NET_FLUX: ((fh + fw,), np.float32), SHADE: ((2,) + L, np.uint32),
+        NET_FLUX: ((fh + fw,), np.float32), SHADE: ((2,) + L, np.uint32), PRESSURE_LO: (F, np.float32),
     }
