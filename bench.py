@@ -532,6 +532,18 @@ def run_mixed(args, local):
     for _ in range(4):  # per-solve iteration counts of a few more steps
         w.encode_steps(1)
         iters.append(w.solve_info())
+    # per-kernel device time of two steps (the solve then runs its loops from
+    # the host, one launch per kernel)
+    w.enable_kernel_timing(True)
+    kern = {}
+    for _ in range(2):
+        w.encode_steps(1)
+        for name, launches, kms, b in w.read_kernel_timing():
+            e = kern.setdefault(name, [0, 0.0])
+            e[0] += launches
+            e[1] += kms
+    w.enable_kernel_timing(False)
+    top = sorted(kern.items(), key=lambda kv: -kv[1][1])[:16]
     water = w.read(rw.SOLID_MASK) == 0
     p = w.read(rw.PRESSURE).astype(np.float64) + w.read(rw.PRESSURE_LO).astype(np.float64)
     rho = fp.rel_residual(p, w.read(rw.DIVERGENCE), water)
@@ -541,6 +553,7 @@ def run_mixed(args, local):
         "world_steps_per_s": steps / (ms / 1000.0), "ms_per_step": ms / steps, "steps": steps,
         "solves": [{"outer": o, "cg_iterations": i, "rel_residual_device": r} for o, i, r in iters],
         "rel_residual_fp64_host": rho, "tolerance": 1e-5,
+        "kernels_ms_per_step": [[k, round(v[1] / 2, 4), v[0] // 2] for k, v in top],
     }
 
 

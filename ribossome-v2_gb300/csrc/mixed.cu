@@ -86,6 +86,7 @@ struct MpCtl {
   int converged, inner_done;
   int max_outer, max_inner;
   int ncomp;
+  int big;            // the largest water component
   float tol2, itol2;  // squared relative tolerances
   float rz, alpha, beta;
   float scale[2];     // V-cycle input scale and its inverse
@@ -106,10 +107,14 @@ struct MpArgs {
   const int* label;     // component per cell (-1: wall)
   float *r, *e, *d, *q, *z;
   float* part;          // per-block partial sums [blocks][2]
+  double* part_c;       // per-block sum over the block's dominant component
+  int* part_dom;        // per-block dominant component (-1: none)
   MpCtl* ctl;
   double* comp_sum_r;
   double* comp_sum_z;
   double* comp_mean;
+  float* comp_mean_f;   // FP32 copies for the per-cell passes
+  float* comp_shift;    // per component: mean of z + mean of r / eps0
   const double* comp_size;
 };
 
@@ -168,9 +173,12 @@ __device__ __forceinline__ void total_partials(const MpArgs& a, float& t0, float
   const int tid = threadIdx.y * BX + threadIdx.x;
   const unsigned n = gridDim.x * gridDim.y;
   float v0 = 0.0f, v1 = 0.0f;
+  const float2* part = reinterpret_cast<const float2*>(a.part);
+#pragma unroll 8
   for (unsigned b = tid; b < n; b += NT) {
-    v0 += ((volatile float*)a.part)[2 * b];
-    v1 += ((volatile float*)a.part)[2 * b + 1];
+    const float2 pv = __ldcg(part + b);  // L2: the other blocks' partials
+    v0 += pv.x;
+    v1 += pv.y;
   }
   s0[tid] = v0;
   s1[tid] = v1;
@@ -187,9 +195,12 @@ __device__ __forceinline__ void total_partials(const MpArgs& a, float& t0, float
   __syncthreads();
 }
 
-// Per-component FP64 sums of a per-cell value (block-aggregated for the
-// block's first water component).
-__device__ __forceinline__ void comp_add(const MpArgs& a, double* sums, const Cell& c, double v) {
+// Per-component FP64 sums of a per-cell value.  The block sums the cells of its dominant component (that of its first
+// water cell) and records that partial with the component; cells of other
+// components (rare: the block straddles a rock wall) add directly.  The last
+// block gathers the partials (comp_gather), so no address receives an atomic
+// from every block.
+__device__ __forceinline__ void comp_add(const MpArgs& a, double* sums, const Cell& c, float v) {
   __shared__ int dom;
   __shared__ double sh[NT / 32];
   const int tid = threadIdx.y * BX + threadIdx.x;
@@ -203,21 +214,50 @@ __device__ __forceinline__ void comp_add(const MpArgs& a, double* sums, const Ce
     dom = dm;
   }
   __syncthreads();
-  double own = 0.0;
+  float own = 0.0f;
   if (c.water) {
     const int lab = a.label[c.i];
     if (lab == dom) own = v;
-    else atomicAdd(sums + lab, v);
+    else atomicAdd(sums + lab, (double)v);
   }
-  for (int o = 16; o > 0; o >>= 1) own += __shfl_down_sync(0xffffffffu, own, o);
-  if ((tid & 31) == 0) sh[tid >> 5] = own;
+  double dv = (double)own;
+  for (int o = 16; o > 0; o >>= 1) dv += __shfl_down_sync(0xffffffffu, dv, o);
+  if ((tid & 31) == 0) sh[tid >> 5] = dv;
   __syncthreads();
-  if (tid == 0 && dom >= 0) {
+  if (tid == 0) {
     double t = 0.0;
     for (int w = 0; w < NT / 32; w++) t += sh[w];
-    atomicAdd(sums + dom, t);
+    const unsigned b = blockIdx.y * gridDim.x + blockIdx.x;
+    a.part_c[b] = t;
+    a.part_dom[b] = dom;
   }
-  __threadfence();  // the sums are complete before this block counts itself done
+  __threadfence();  // partials and direct adds land before this block counts itself done
+}
+
+// In the last block: every block's partial added to its component's sum --
+// the largest component's in a fixed order (deterministic), the others
+// (few) with atomics -- complete and visible when this returns.
+__device__ __forceinline__ void comp_gather(const MpArgs& a, double* sums, unsigned nblocks) {
+  __shared__ double sh[NT];
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  const int big = a.ctl->big;
+  double acc = 0.0;
+#pragma unroll 8
+  for (unsigned b = tid; b < nblocks; b += NT) {
+    const int d = __ldcg(a.part_dom + b);
+    const double v = __ldcg(a.part_c + b);
+    if (d == big) acc += v;
+    else if (d >= 0) atomicAdd(sums + d, v);
+  }
+  sh[tid] = acc;
+  __syncthreads();
+  for (int o = NT / 2; o > 0; o >>= 1) {
+    if (tid < o) sh[tid] += sh[tid + o];
+    __syncthreads();
+  }
+  if (tid == 0 && big >= 0) sums[big] += sh[0];
+  __threadfence();
+  __syncthreads();
 }
 
 // In the last block: component means of the residual (FP64) and the power-of-
@@ -226,8 +266,11 @@ __device__ __forceinline__ void finish_residual_stats(const MpArgs& a, float rn2
   const int tid = threadIdx.y * BX + threadIdx.x;
   MpCtl* ctl = a.ctl;
   const int nc = ctl->ncomp;
+  comp_gather(a, a.comp_sum_r, gridDim.x * gridDim.y);
   for (int c = tid; c < nc; c += NT) {
-    a.comp_mean[c] = a.comp_size[c] > 0.0 ? __ldcg(a.comp_sum_r + c) / a.comp_size[c] : 0.0;
+    const double m = a.comp_size[c] > 0.0 ? __ldcg(a.comp_sum_r + c) / a.comp_size[c] : 0.0;
+    a.comp_mean[c] = m;
+    a.comp_mean_f[c] = (float)m;
     a.comp_sum_r[c] = 0.0;
   }
   if (tid == 0) {
@@ -243,8 +286,10 @@ __device__ __forceinline__ void finish_residual_stats(const MpArgs& a, float rn2
   }
 }
 
+// `graph` = 1 when the kernel runs inside the solve's graph (it then sets the
+// loop conditions); 0 when the host drives the loops.
 __global__ void k_mp_begin(MpArgs a, int max_outer, int max_inner, float tol, float itol,
-                           cudaGraphConditionalHandle h_outer) {
+                           cudaGraphConditionalHandle h_outer, int graph) {
   MpCtl* ctl = a.ctl;
   for (int c = threadIdx.x; c < ctl->ncomp; c += blockDim.x) {
     a.comp_sum_r[c] = 0.0;
@@ -260,14 +305,14 @@ __global__ void k_mp_begin(MpArgs a, int max_outer, int max_inner, float tol, fl
     ctl->itol2 = itol * itol;
     ctl->bn2 = 0.0;
     ctl->rho = 0.0;
-    cudaGraphSetConditional(h_outer, 1u);
+    if (graph) cudaGraphSetConditional(h_outer, 1u);
   }
 }
 
 // Outer residual r = rhs - L(hi + lo) in FP32-pair arithmetic; the CG
 // starts from e = 0 on it.  The last block decides both loops.
 __global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphConditionalHandle h_outer,
-                                                    cudaGraphConditionalHandle h_inner, int final_pass) {
+                                                    cudaGraphConditionalHandle h_inner, int final_pass, int graph) {
   const Cell c = cell_of(a);
   float rf = 0.0f, b = 0.0f;
   if (c.water) {
@@ -291,7 +336,7 @@ __global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphCondition
     a.r[c.i] = rf;
     a.e[c.i] = 0.0f;
   }
-  comp_add(a, a.comp_sum_r, c, (double)rf);
+  if (!final_pass) comp_add(a, a.comp_sum_r, c, rf);
   if (!block_partials(a, rf * rf, b * b)) return;
   float rn2, bn2;
   total_partials(a, rn2, bn2);
@@ -321,8 +366,10 @@ __global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphCondition
     ctl->itarget2 = (float)(need > (double)ctl->itol2 ? (need < 1.0 ? need : 1.0) : (double)ctl->itol2);
     ctl->outer += 1;
     ctl->done = 0;
-    cudaGraphSetConditional(h_inner, conv ? 0u : 1u);
-    cudaGraphSetConditional(h_outer, (!conv && ctl->outer < ctl->max_outer) ? 1u : 0u);
+    if (graph) {
+      cudaGraphSetConditional(h_inner, conv ? 0u : 1u);
+      cudaGraphSetConditional(h_outer, (!conv && ctl->outer < ctl->max_outer) ? 1u : 0u);
+    }
   }
 }
 
@@ -332,9 +379,7 @@ __global__ void __launch_bounds__(NT) k_mp_dots(MpArgs a) {
   const Cell c = cell_of(a);
   float zr = 0.0f, zq = 0.0f;
   if (c.water) {
-    const int lab = a.label[c.i];
-    const double zm = a.comp_size[lab] > 0.0 ? a.comp_sum_z[lab] / a.comp_size[lab] : 0.0;
-    const float zc = (float)((double)a.z[c.i] - zm - a.comp_mean[lab] / (double)a.eps0);
+    const float zc = a.z[c.i] - a.comp_shift[a.label[c.i]];
     a.z[c.i] = zc;
     zr = zc * a.r[c.i];
     zq = zc * a.q[c.i];
@@ -346,11 +391,25 @@ __global__ void __launch_bounds__(NT) k_mp_dots(MpArgs a) {
   total_partials(a, tzr, tzq);
   MpCtl* ctl = a.ctl;
   const int tid = threadIdx.y * BX + threadIdx.x;
-  for (int k = tid; k < ctl->ncomp; k += NT) a.comp_sum_z[k] = 0.0;
   if (tid == 0) {
     ctl->beta = (ctl->inner == 0 || ctl->rz == 0.0f) ? 0.0f : -ctl->alpha * tzq / ctl->rz;
     ctl->rz = tzr;
     ctl->done = 0;
+  }
+}
+
+// After the V-cycle (one block): gathers the per-tile sums of z the level-0
+// post kernel recorded, and forms each component's shift = mean of z + mean
+// of the residual / eps0 in FP64 (the mean removal), which the next kernel
+// subtracts in FP32.
+__global__ void __launch_bounds__(NT) k_mp_zshift(MpArgs a, unsigned ntiles) {
+  comp_gather(a, a.comp_sum_z, ntiles);
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  const int nc = a.ctl->ncomp;
+  for (int c = tid; c < nc; c += NT) {
+    const double zm = a.comp_size[c] > 0.0 ? __ldcg(a.comp_sum_z + c) / a.comp_size[c] : 0.0;
+    a.comp_shift[c] = (float)(zm + a.comp_mean[c] / (double)a.eps0);
+    a.comp_sum_z[c] = 0.0;
   }
 }
 
@@ -392,7 +451,7 @@ __global__ void __launch_bounds__(NT) k_mp_matvec(MpArgs a) {
 
 // e += alpha d, r -= alpha q; the last block tests the inner tolerance,
 // prepares the next preconditioner input and sets the inner loop condition.
-__global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHandle h_inner) {
+__global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHandle h_inner, int graph) {
   const Cell c = cell_of(a);
   const float alpha = a.ctl->alpha;
   float rn = 0.0f;
@@ -401,7 +460,7 @@ __global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHa
     rn = a.r[c.i] - alpha * a.q[c.i];
     a.r[c.i] = rn;
   }
-  comp_add(a, a.comp_sum_r, c, (double)rn);
+  comp_add(a, a.comp_sum_r, c, rn);
   if (!block_partials(a, rn * rn, 0.0f)) return;
   float rn2, unused;
   total_partials(a, rn2, unused);
@@ -414,7 +473,7 @@ __global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHa
     const bool done = rn2 <= ctl->itarget2 * ctl->r0n2 || !(rn2 == rn2);
     ctl->inner_done = done ? 1 : 0;
     ctl->done = 0;
-    cudaGraphSetConditional(h_inner, (!done && ctl->inner < ctl->max_inner) ? 1u : 0u);
+    if (graph) cudaGraphSetConditional(h_inner, (!done && ctl->inner < ctl->max_inner) ? 1u : 0u);
   }
 }
 
@@ -442,6 +501,9 @@ struct MixedSolver {
   int* label = nullptr;
   MpCtl* ctl = nullptr;
   double *comp_sum_r = nullptr, *comp_sum_z = nullptr, *comp_mean = nullptr, *comp_size = nullptr;
+  float *comp_mean_f = nullptr, *comp_shift = nullptr;
+  double* part_c = nullptr;
+  int* part_dom = nullptr;
   double* inv = nullptr;
   int coarsest_cells = 0;
   MpHierarchy h{};
@@ -479,6 +541,10 @@ MpArgs mp_args(const World& w, const MixedSolver& m) {
   a.comp_sum_z = m.comp_sum_z;
   a.comp_mean = m.comp_mean;
   a.comp_size = m.comp_size;
+  a.comp_mean_f = m.comp_mean_f;
+  a.comp_shift = m.comp_shift;
+  a.part_c = m.part_c;
+  a.part_dom = m.part_dom;
   return a;
 }
 
@@ -513,7 +579,7 @@ cudaError_t capture_solve(World& w, MixedSolver& m, cudaStream_t s) {
   cudaGraphConditionalHandle ho, hi;
   RB_CK(cudaGraphConditionalHandleCreate(&ho, g, 0, 0));
   k_mp_begin<<<1, 256, 0, s>>>(a, setting_or(st.mixed_max_outer, 4), setting_or(st.mixed_max_inner, 64),
-                               setting_or(st.mixed_tol, 1e-5f), setting_or(st.mixed_inner_tol, 1e-3f), ho);
+                               setting_or(st.mixed_tol, 1e-5f), setting_or(st.mixed_inner_tol, 1e-3f), ho, 1);
   RB_CK(cudaGetLastError());
   RB_CK(cudaStreamGetCaptureInfo(s, &cs, &id, &g, &deps, &ed, &nd));
   cudaGraphNodeParams po = {};
@@ -531,7 +597,7 @@ cudaError_t capture_solve(World& w, MixedSolver& m, cudaStream_t s) {
   // outer body: residual, inner loop, update
   cudaStream_t so = m.cap[1];
   RB_CK(cudaStreamBeginCaptureToGraph(so, body_o, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  k_mp_residual<<<grid, blk, 0, so>>>(a, ho, hi, 0);
+  k_mp_residual<<<grid, blk, 0, so>>>(a, ho, hi, 0, 1);
   cudaGraph_t gb = nullptr;
   RB_CK(cudaStreamGetCaptureInfo(so, &cs, &id, &gb, &deps, &ed, &nd));
   cudaGraphNodeParams pi = {};
@@ -554,14 +620,58 @@ cudaError_t capture_solve(World& w, MixedSolver& m, cudaStream_t s) {
   h.alpha = setting_or(st.mixed_alpha, 1.8f);
   h.pre = (int)w.cfg.mg_pre;
   h.post = (int)w.cfg.mg_post;
-  launch_mixed_vcycle(w.dev(), w.levels.data(), (int)w.levels.size(), w.mg, h, si);
+  const int tiles = launch_mixed_vcycle(w.dev(), w.levels.data(), (int)w.levels.size(), w.mg, h, si);
+  k_mp_zshift<<<1, blk, 0, si>>>(a, (unsigned)tiles);
   k_mp_dots<<<grid, blk, 0, si>>>(a);
   k_mp_direction<<<grid, blk, 0, si>>>(a);
   k_mp_matvec<<<grid, blk, 0, si>>>(a);
-  k_mp_axpy<<<grid, blk, 0, si>>>(a, hi);
+  k_mp_axpy<<<grid, blk, 0, si>>>(a, hi, 1);
   RB_CK(cudaStreamEndCapture(si, &tmp));
 
-  k_mp_residual<<<grid, blk, 0, s>>>(a, ho, hi, 1);  // residual of the result
+  k_mp_residual<<<grid, blk, 0, s>>>(a, ho, hi, 1, 1);  // residual of the result
+  return cudaGetLastError();
+}
+
+// The same solve with the loops driven from the host (one wait per
+// iteration to read the loop state): every kernel is launched on its own,
+// so kernel timing and profilers see each of them.
+cudaError_t direct_solve(World& w, MixedSolver& m) {
+  const MpArgs a = mp_args(w, m);
+  cudaStream_t s = w.stream;
+  const dim3 grid((w.fw + BX - 1) / BX, (w.fh + BY - 1) / BY), blk(BX, BY);
+  const ribo_world_settings& st = w.st;
+  const int max_outer = setting_or(st.mixed_max_outer, 4), max_inner = setting_or(st.mixed_max_inner, 64);
+  const double F = (double)w.fcells();
+  MpHierarchy h = m.h;
+  h.alpha = setting_or(st.mixed_alpha, 1.8f);
+  h.pre = (int)w.cfg.mg_pre;
+  h.post = (int)w.cfg.mg_post;
+  cudaGraphConditionalHandle none = 0;
+  RB_LAUNCH("mp_begin", 0.0, s,
+            k_mp_begin<<<1, 256, 0, s>>>(a, max_outer, max_inner, setting_or(st.mixed_tol, 1e-5f),
+                                         setting_or(st.mixed_inner_tol, 1e-3f), none, 0));
+  MpCtl c{};
+  auto read_ctl = [&]() {
+    cudaError_t e = cudaMemcpyAsync(&c, m.ctl, sizeof c, cudaMemcpyDeviceToHost, s);
+    return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+  };
+  for (int o = 0; o < max_outer; o++) {
+    RB_LAUNCH("mp_residual", 25.0 * F, s, k_mp_residual<<<grid, blk, 0, s>>>(a, none, none, 0, 0));
+    RB_CK(read_ctl());
+    if (c.converged) break;
+    for (int i = 0; i < max_inner; i++) {
+      const int tiles = launch_mixed_vcycle(w.dev(), w.levels.data(), (int)w.levels.size(), w.mg, h, s);
+      RB_LAUNCH("mp_zshift", 0.0, s, k_mp_zshift<<<1, blk, 0, s>>>(a, (unsigned)tiles));
+      RB_LAUNCH("mp_dots", 17.0 * F, s, k_mp_dots<<<grid, blk, 0, s>>>(a));
+      RB_LAUNCH("mp_direction", 13.0 * F, s, k_mp_direction<<<grid, blk, 0, s>>>(a));
+      RB_LAUNCH("mp_matvec", 9.0 * F, s, k_mp_matvec<<<grid, blk, 0, s>>>(a));
+      RB_LAUNCH("mp_axpy", 29.0 * F, s, k_mp_axpy<<<grid, blk, 0, s>>>(a, none, 0));
+      RB_CK(read_ctl());
+      if (c.inner_done) break;
+    }
+    RB_LAUNCH("mp_update", 21.0 * F, s, k_mp_update<<<grid, blk, 0, s>>>(a));
+  }
+  RB_LAUNCH("mp_residual", 25.0 * F, s, k_mp_residual<<<grid, blk, 0, s>>>(a, none, none, 1, 0));
   return cudaGetLastError();
 }
 
@@ -598,6 +708,10 @@ ribo_status mixed_init(World& w) {
   MP_ALLOC(m->comp_sum_z, COMP_CAP * 8);
   MP_ALLOC(m->comp_mean, COMP_CAP * 8);
   MP_ALLOC(m->comp_size, COMP_CAP * 8);
+  MP_ALLOC(m->comp_mean_f, COMP_CAP * 4);
+  MP_ALLOC(m->comp_shift, COMP_CAP * 4);
+  MP_ALLOC(m->part_c, blocks * 8);
+  MP_ALLOC(m->part_dom, blocks * 4);
   m->coarsest_cells = last.nx * last.ny;
   MP_ALLOC(m->inv, (size_t)m->coarsest_cells * m->coarsest_cells * 8);
   const int nh = half_levels(w);
@@ -614,7 +728,9 @@ ribo_status mixed_init(World& w) {
 #undef MP_ALLOC
   m->h.r = m->r;
   m->h.label = m->label;
-  m->h.comp_mean = m->comp_mean;
+  m->h.comp_mean = m->comp_mean_f;
+  m->h.part_c = m->part_c;
+  m->h.part_dom = m->part_dom;
   m->h.scale = reinterpret_cast<const float*>(reinterpret_cast<const char*>(m->ctl) + offsetof(MpCtl, scale));
   m->h.z = m->z;
   m->h.comp_sum_z = m->comp_sum_z;
@@ -633,7 +749,7 @@ size_t mixed_footprint(const ribo_world_cfg& c, const std::vector<MgLevel>& leve
   const int nl = (int)levels.size();
   const int k = multigrid_first_coarse_level(levels.data(), nl);
   const size_t nc = (size_t)levels[nl - 1].nx * levels[nl - 1].ny;
-  size_t b = F * 4 * 7 + blocks * 8 + sizeof(MpCtl) + (size_t)COMP_CAP * 8 * 4 + nc * nc * 8;
+  size_t b = F * 4 * 7 + blocks * (8 + 8 + 4) + sizeof(MpCtl) + (size_t)COMP_CAP * (8 * 4 + 4 * 2) + nc * nc * 8;
   const int nh = k < HALF_LEVELS ? k : HALF_LEVELS;
   for (int l = 0; l < k; l++) {
     const size_t n = (size_t)levels[l].nx * levels[l].ny, es = l < nh ? 2 : 4;
@@ -770,6 +886,9 @@ ribo_status mixed_setup(World& w) {
   double nwater = 0.0;
   for (int c = 0; c < ncomp; c++) nwater += size[c];
   ctl.nwater = (float)nwater;
+  ctl.big = -1;
+  for (int c = 0; c < ncomp; c++)
+    if (ctl.big < 0 || size[c] > size[ctl.big]) ctl.big = c;
   ctl.scale[0] = ctl.scale[1] = 1.0f;
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->ctl, &ctl, sizeof ctl, cudaMemcpyHostToDevice, w.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(w.stream);
@@ -788,6 +907,7 @@ ribo_status mixed_solve(World& w) {
     e = capture_solve(w, *m, w.stream);
     return cuda_status(e, "mixed solve capture");
   }
+  if (w.cfg.no_graphs || w.timing) return cuda_status(direct_solve(w, *m), "mixed solve");
   if (m->standalone && memcmp(&m->built_for, &w.st, sizeof w.st) != 0) {
     cudaGraphExecDestroy(m->standalone);
     m->standalone = nullptr;

@@ -480,8 +480,8 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
     const float* r = R + cs.off[l];
     const uint8_t* f = F + cs.off[l];
     for (int k = 0; k < nu_pre; k++) {
-      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p, r, f, 0u);
-      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p, r, f, 1u);
+      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p,r, f, 0u);
+      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p,r, f, 1u);
     }
     const int nx = cs.nx[l], ny = cs.ny[l], cnx = cs.nx[l + 1], cny = cs.ny[l + 1];
     float* pc = P + cs.off[l + 1];
@@ -548,8 +548,8 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
     __syncthreads();
     const uint32_t c0 = MP ? 1u : 0u;
     for (int k = 0; k < nu_post; k++) {
-      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, c0);
-      sm_sweep(nx, cs.ny[l], cs.eps[l], p, r, f, c0 ^ 1u);
+      sm_sweep(nx, cs.ny[l], cs.eps[l], p,r, f, c0);
+      sm_sweep(nx, cs.ny[l], cs.eps[l], p,r, f, c0 ^ 1u);
     }
   }
   {
@@ -1002,10 +1002,12 @@ struct MpLevelArgs {
   float alpha;
   // level 0
   const int* label;          // water component of each cell (-1: wall)
-  const double* comp_mean;   // mean of the CG residual per component
+  const float* comp_mean;    // mean of the CG residual per component
   const float* scale;        // [0] scale applied to the residual, [1] its inverse
   float* z;                  // V-cycle output, unscaled
-  double* comp_sum_z;        // per-component sums of z
+  double* comp_sum_z;        // per-component sums of z (cells outside a tile's dominant component)
+  double* part_c;            // per tile: sum of z over the tile's dominant component
+  int* part_dom;             // per tile: that component (-1: none)
 };
 
 __device__ __forceinline__ float mp_ld(const float* p, size_t i) { return p[i]; }
@@ -1013,38 +1015,41 @@ __device__ __forceinline__ float mp_ld(const __half* p, size_t i) { return __hal
 __device__ __forceinline__ void mp_st(float* p, size_t i, float v) { p[i] = v; }
 __device__ __forceinline__ void mp_st(__half* p, size_t i, float v) { p[i] = __float2half_rn(v); }
 
-// The level's right-hand side at a water cell; level 0 removes the
-// component mean (FP64) and applies the FP16 scale.
-template <bool TOP, class T>
-__device__ __forceinline__ float mp_rhs(const MpLevelArgs& a, size_t gi, float sc) {
-  if (TOP) {
-    const double r = (double)static_cast<const float*>(a.rhs)[gi];
-    return (float)((r - a.comp_mean[a.label[gi]]) * (double)sc);
-  }
-  return mp_ld(static_cast<const T*>(a.rhs), gi);
-}
-
+// Loads the box of a level: the right-hand side (level 0: the CG residual
+// minus its component's mean, times the FP16 scale), the water flags and,
+// for post-smoothing, e_f plus alpha times the coarse total correction.
 template <int TW, int TH, bool TOP, class T>
-__device__ __forceinline__ void mp_load(const MpLevelArgs& a, int bx, int by, int RH, bool post, float* sp, float* sr,
-                                        uint8_t* sf) {
+__device__ __forceinline__ void mp_load(const MpLevelArgs& a, int bx, int by, int H, int RH, bool post, float* sp,
+                                        float* sr, uint8_t* sf) {
+  // Only the columns the sweeps and the restriction touch (H cells either
+  // side of the tile); the alignment margin of the TMA box stays unused.
+  // Every load is issued unconditionally (clamped index) so they overlap.
   constexpr int BOXW = TW + 2 * BOXX;
-  const int n = BOXW * RH, tid = threadIdx.y * BX + threadIdx.x;
+  const int W = TW + 2 * H, i0 = BOXX - H;
+  const int n = W * RH, tid = threadIdx.y * BX + threadIdx.x;
   const float sc = TOP ? a.scale[0] : 1.0f;
   for (int e = tid; e < n; e += BX * BY) {
-    const int gx = bx + e % BOXW, gy = by + e / BOXW;
-    float p = 0.0f, r = 0.0f;
-    uint8_t f = 0;
-    if (gx >= 0 && gy >= 0 && gx < a.nx && gy < a.ny) {
-      const size_t gi = (size_t)gy * a.nx + gx;
-      f = a.fl[gi];
-      if (f) {
-        r = mp_rhs<TOP, T>(a, gi, sc);
-        if (post) p = mp_ld(static_cast<const T*>(a.ef), gi) + a.alpha * a.cE[(size_t)(gy / 2) * a.cnx + gx / 2];
-      }
+    const int i = i0 + e % W, j = e / W;
+    const int gx = bx + i, gy = by + j;
+    const bool in = gx >= 0 && gy >= 0 && gx < a.nx && gy < a.ny;
+    const size_t gi = in ? (size_t)gy * a.nx + gx : 0;
+    const uint8_t f = in ? a.fl[gi] : 0;
+    float r, p = 0.0f;
+    if (TOP) {
+      const float rr = static_cast<const float*>(a.rhs)[gi];
+      const int lab = a.label[gi];
+      r = (rr - a.comp_mean[lab < 0 ? 0 : lab]) * sc;
+    } else {
+      r = mp_ld(static_cast<const T*>(a.rhs), gi);
     }
-    sp[e] = p;
-    sr[e] = r;
-    sf[e] = f;
+    if (post) {
+      const size_t ci = in ? (size_t)(gy / 2) * a.cnx + gx / 2 : 0;
+      p = mp_ld(static_cast<const T*>(a.ef), gi) + a.alpha * a.cE[ci];
+    }
+    const int c = j * BOXW + i;
+    sp[c] = f ? p : 0.0f;
+    sr[c] = f ? r : 0.0f;
+    sf[c] = f;
   }
   __syncthreads();
 }
@@ -1059,7 +1064,7 @@ __global__ void __launch_bounds__(BX* BY) k_mp_pre(const __grid_constant__ MpLev
   float* sr = sp + BOXW * RH;
   uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
   const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, bx = x0 - BOXX, by = y0 - H;
-  mp_load<TW, TH, TOP, T>(a, bx, by, RH, false, sp, sr, sf);
+  mp_load<TW, TH, TOP, T>(a, bx, by, H, RH, false, sp, sr, sf);
   box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, a.eps, sp, sr, sf, 0);
   T* ef = static_cast<T*>(a.ef);
   for (int j = threadIdx.y; j < TH; j += BY)
@@ -1090,26 +1095,6 @@ __global__ void __launch_bounds__(BX* BY) k_mp_pre(const __grid_constant__ MpLev
     }
 }
 
-// Per-block sums of a per-cell value into per-component FP64 accumulators:
-// the block's dominant component (that of its first water cell) is summed in
-// shared memory and added once; cells of other components add directly.
-__device__ __forceinline__ void comp_accumulate(double* comp_sum, int dom, int lab, double v, double* sh) {
-  double own = 0.0;
-  if (lab >= 0) {
-    if (lab == dom) own = v;
-    else atomicAdd(comp_sum + lab, v);
-  }
-  for (int o = 16; o > 0; o >>= 1) own += __shfl_down_sync(0xffffffffu, own, o);
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nw = (blockDim.x * blockDim.y) >> 5;
-  if ((tid & 31) == 0) sh[tid >> 5] = own;
-  __syncthreads();
-  if (tid == 0 && dom >= 0) {
-    double t = 0.0;
-    for (int w = 0; w < nw; w++) t += sh[w];
-    atomicAdd(comp_sum + dom, t);
-  }
-}
-
 // Prolong (alpha * coarse total) + post-smooth (colours reversed).
 template <int TW, int TH, bool TOP, class T>
 __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLevelArgs a, int nu) {
@@ -1122,7 +1107,7 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
   float* sr = sp + BOXW * RH;
   uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
   const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, bx = x0 - BOXX, by = y0 - H;
-  mp_load<TW, TH, TOP, T>(a, bx, by, RH, true, sp, sr, sf);
+  mp_load<TW, TH, TOP, T>(a, bx, by, H, RH, true, sp, sr, sf);
   box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, a.eps, sp, sr, sf, 1);
   if (!TOP) {
     for (int j = threadIdx.y; j < TH; j += BY)
@@ -1143,7 +1128,7 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
   }
   __syncthreads();
   const float inv = a.scale[1];
-  double own = 0.0;
+  float own = 0.0f;
   for (int j = threadIdx.y; j < TH; j += BY)
     for (int i = threadIdx.x; i < TW; i += BX) {
       const int gx = x0 + i, gy = y0 + j;
@@ -1153,11 +1138,23 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
       const float z = lab >= 0 ? sp[(j + H) * BOXW + i + BOXX] * inv : 0.0f;
       a.z[gi] = z;
       if (lab >= 0) {
-        if (lab == dom) own += (double)z;
+        if (lab == dom) own += z;
         else atomicAdd(a.comp_sum_z + lab, (double)z);
       }
     }
-  comp_accumulate(a.comp_sum_z, dom, dom, own, zsh);
+  // the tile's partial for its dominant component (FP64 above the thread level)
+  double t = (double)own;
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  if ((tid & 31) == 0) zsh[tid >> 5] = t;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < BX * BY / 32; w++) s += zsh[w];
+    const unsigned b = blockIdx.y * gridDim.x + blockIdx.x;
+    a.part_c[b] = s;
+    a.part_dom[b] = dom;
+  }
 }
 
 template <int TW, int TH>
@@ -1174,26 +1171,42 @@ void mp_attrs(int mx) {
   cudaFuncSetAttribute(k_mp_post<TW, TH, false, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
+const char* const MP_PRE_NAMES[8] = {"mp_pre_L0", "mp_pre_L1", "mp_pre_L2", "mp_pre_L3",
+                                     "mp_pre_L4", "mp_pre_L5", "mp_pre_L6", "mp_pre_L7+"};
+const char* const MP_POST_NAMES[8] = {"mp_post_L0", "mp_post_L1", "mp_post_L2", "mp_post_L3",
+                                      "mp_post_L4", "mp_post_L5", "mp_post_L6", "mp_post_L7+"};
+
+// Algorithmic bytes: level 0 reads the CG residual (4), the component label
+// (4) and the water flag (1); levels >= 1 their rhs (2 or 4) and flag; the
+// correction is written (2 or 4), the coarse rhs written (a quarter size);
+// post reads e_f, rhs, flag and a quarter-size coarse total and writes the
+// total (z and its label read on level 0).
 template <int TW, int TH>
-void mp_launch_pre(const MpLevelArgs& a, bool top, bool half, bool chalf, int nu, cudaStream_t s) {
+void mp_launch_pre(const MpLevelArgs& a, int l, bool top, bool half, bool chalf, int nu, cudaStream_t s) {
   const dim3 grid((a.nx + TW - 1) / TW, (a.ny + TH - 1) / TH), blk(BX, BY);
   const size_t sm = box_smem<TW, TH>(2 * nu + 1);
-  if (top && half && chalf) k_mp_pre<TW, TH, true, __half, __half><<<grid, blk, sm, s>>>(a, nu);
-  else if (top && half) k_mp_pre<TW, TH, true, __half, float><<<grid, blk, sm, s>>>(a, nu);
-  else if (top) k_mp_pre<TW, TH, true, float, float><<<grid, blk, sm, s>>>(a, nu);
-  else if (half && chalf) k_mp_pre<TW, TH, false, __half, __half><<<grid, blk, sm, s>>>(a, nu);
-  else if (half) k_mp_pre<TW, TH, false, __half, float><<<grid, blk, sm, s>>>(a, nu);
-  else k_mp_pre<TW, TH, false, float, float><<<grid, blk, sm, s>>>(a, nu);
+  const double es = half ? 2.0 : 4.0, n = (double)a.nx * a.ny;
+  const double bytes = n * ((top ? 9.0 : es + 1.0) + es + (chalf ? 2.0 : 4.0) / 4.0);
+  const char* name = MP_PRE_NAMES[l < 7 ? l : 7];
+  if (top && half && chalf) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, true, __half, __half><<<grid, blk, sm, s>>>(a, nu));
+  else if (top && half) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, true, __half, float><<<grid, blk, sm, s>>>(a, nu));
+  else if (top) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, true, float, float><<<grid, blk, sm, s>>>(a, nu));
+  else if (half && chalf) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, false, __half, __half><<<grid, blk, sm, s>>>(a, nu));
+  else if (half) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, false, __half, float><<<grid, blk, sm, s>>>(a, nu));
+  else RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, false, float, float><<<grid, blk, sm, s>>>(a, nu));
 }
 
 template <int TW, int TH>
-void mp_launch_post(const MpLevelArgs& a, bool top, bool half, int nu, cudaStream_t s) {
+void mp_launch_post(const MpLevelArgs& a, int l, bool top, bool half, int nu, cudaStream_t s) {
   const dim3 grid((a.nx + TW - 1) / TW, (a.ny + TH - 1) / TH), blk(BX, BY);
   const size_t sm = box_smem<TW, TH>(2 * nu);
-  if (top && half) k_mp_post<TW, TH, true, __half><<<grid, blk, sm, s>>>(a, nu);
-  else if (top) k_mp_post<TW, TH, true, float><<<grid, blk, sm, s>>>(a, nu);
-  else if (half) k_mp_post<TW, TH, false, __half><<<grid, blk, sm, s>>>(a, nu);
-  else k_mp_post<TW, TH, false, float><<<grid, blk, sm, s>>>(a, nu);
+  const double es = half ? 2.0 : 4.0, n = (double)a.nx * a.ny;
+  const double bytes = n * (es + (top ? 9.0 : es + 1.0) + 1.0 + (top ? 8.0 : 4.0));
+  const char* name = MP_POST_NAMES[l < 7 ? l : 7];
+  if (top && half) RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, true, __half><<<grid, blk, sm, s>>>(a, nu));
+  else if (top) RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, true, float><<<grid, blk, sm, s>>>(a, nu));
+  else if (half) RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, false, __half><<<grid, blk, sm, s>>>(a, nu));
+  else RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, false, float><<<grid, blk, sm, s>>>(a, nu));
 }
 
 }  // namespace
@@ -1234,13 +1247,18 @@ int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBuf
     a.scale = h.scale;
     a.z = h.z;
     a.comp_sum_z = h.comp_sum_z;
+    a.part_c = h.part_c;
+    a.part_dom = h.part_dom;
     return a;
   };
+  const bool small0 = small_tiles(levels[0]);
+  const int tw0 = small0 ? 32 : 64, th0 = small0 ? 16 : 32;
+  const int tiles0 = ((levels[0].nx + tw0 - 1) / tw0) * ((levels[0].ny + th0 - 1) / th0);
   for (int l = 0; l < k; l++) {
     const MpLevelArgs a = args(l);
     const bool half = l < h.nhalf, chalf = l + 1 < k && l + 1 < h.nhalf;
-    if (small_tiles(levels[l])) mp_launch_pre<32, 16>(a, l == 0, half, chalf, h.pre, s);
-    else mp_launch_pre<64, 32>(a, l == 0, half, chalf, h.pre, s);
+    if (small_tiles(levels[l])) mp_launch_pre<32, 16>(a, l, l == 0, half, chalf, h.pre, s);
+    else mp_launch_pre<64, 32>(a, l, l == 0, half, chalf, h.pre, s);
     launches++;
   }
   size_t coarse_smem = 0;
@@ -1248,16 +1266,18 @@ int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBuf
   CoarseOne co{coarse_pass(d, levels, nl, b, &coarse_smem, &coarse_bytes)};
   co.e.inv = h.coarse_inv;
   co.e.alpha = h.alpha;
-  k_mg_coarse<CoarseOne, true><<<1, COARSE_THREADS, coarse_smem, s>>>(co, h.pre, h.post, 0);
+  RB_LAUNCH("mp_coarse_vcycle", coarse_bytes, s,
+            k_mg_coarse<CoarseOne, true><<<1, COARSE_THREADS, coarse_smem, s>>>(co, h.pre, h.post, 0));
   launches++;
   for (int l = k - 1; l >= 0; l--) {
     const MpLevelArgs a = args(l);
     const bool half = l < h.nhalf;
-    if (small_tiles(levels[l])) mp_launch_post<32, 16>(a, l == 0, half, h.post, s);
-    else mp_launch_post<64, 32>(a, l == 0, half, h.post, s);
+    if (small_tiles(levels[l])) mp_launch_post<32, 16>(a, l, l == 0, half, h.post, s);
+    else mp_launch_post<64, 32>(a, l, l == 0, half, h.post, s);
     launches++;
   }
-  return launches;
+  (void)launches;
+  return tiles0;
 }
 
 }  // namespace ribo

@@ -162,17 +162,20 @@ struct MpHierarchy {
   } fine[16];
   const float* r;            // level-0 input: the CG residual
   const int* label;          // water component per fluid cell (-1: wall)
-  const double* comp_mean;   // mean residual per component
+  const float* comp_mean;    // mean residual per component (FP32 copy of the FP64 mean)
   const float* scale;        // [0] scale, [1] inverse scale
   float* z;                  // level-0 output
-  double* comp_sum_z;        // per-component sums of z (accumulated)
+  double* comp_sum_z;        // per-component sums of z (cells outside a tile's dominant component)
+  double* part_c;            // per level-0 tile: sum of z over its dominant component
+  int* part_dom;             // per level-0 tile: that component (-1: none)
   const double* coarse_inv;  // dense FP64 inverse of the coarsest operator
   float alpha;               // coarse-correction over-relaxation
   int pre, post;
 };
 // Sets the kernel attributes of the mixed V-cycle (call before capturing it).
 void multigrid_prepare_mixed();
-// Launches one V-cycle of the preconditioner; returns the launches made.
+// Launches one V-cycle of the preconditioner; returns the number of level-0
+// tiles (entries of part_c / part_dom it wrote).
 int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nlevels, const MgBufs& b, const MpHierarchy& h,
                         cudaStream_t s);
 

@@ -161,8 +161,7 @@ def load_library(path: str = LIB_PATH):
         "ribo_batch_set_tile_modes": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
         "ribo_batch_step_ragged": ([vp, P(SimParams), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_world_footprint": ([P(WorldCfg), P(ctypes.c_uint64)], ctypes.c_int),
-        "ribo_world_solve_info": ([vp, P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_double)], ctypes.c_int),
-        "ribo_world_memory": ([vp, P(ctypes.c_uint64)], ctypes.c_int),
+        "ribo_world_solve_info": ([vp, P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_double)], ctypes.c_int),        "ribo_world_memory": ([vp, P(ctypes.c_uint64)], ctypes.c_int),
         "ribo_server_create": ([P(ServerCfg), P(vp)], ctypes.c_int),
         "ribo_server_destroy": ([vp], None),
         "ribo_server_submit": ([vp, P(Job), P(ctypes.c_uint64)], ctypes.c_int),
