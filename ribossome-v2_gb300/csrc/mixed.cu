@@ -118,20 +118,27 @@ struct MpArgs {
   const double* comp_size;
 };
 
+// The per-cell kernels of the CG run one thread per RR cells of a column:
+// a block covers BX x (BY * RR) cells, which keeps the number of blocks (and
+// of partial sums the last block gathers) small.
+constexpr int RR = 8;
+
 struct Cell {
   int x, y;
   size_t i;
   bool in, water;
 };
-__device__ __forceinline__ Cell cell_of(const MpArgs& a) {
+__device__ __forceinline__ Cell cell_at(const MpArgs& a, int k) {
   Cell c;
   c.x = blockIdx.x * BX + threadIdx.x;
-  c.y = blockIdx.y * BY + threadIdx.y;
+  c.y = (blockIdx.y * RR + k) * BY + threadIdx.y;
   c.in = c.x < a.fw && c.y < a.fh;
   c.i = c.in ? (size_t)c.y * a.fw + c.x : 0;
   c.water = c.in && a.fl[c.i] != 0;
   return c;
 }
+// position of cell k of this thread inside the block's region (row-major)
+__device__ __forceinline__ int cell_pos(int k) { return ((k * BY + (int)threadIdx.y) * BX) + (int)threadIdx.x; }
 
 // Block sums of two values written to the per-block partials; returns true in
 // every thread of the block that finished last (its partials are visible).
@@ -195,30 +202,31 @@ __device__ __forceinline__ void total_partials(const MpArgs& a, float& t0, float
   __syncthreads();
 }
 
-// Per-component FP64 sums of a per-cell value.  The block sums the cells of its dominant component (that of its first
-// water cell) and records that partial with the component; cells of other
-// components (rare: the block straddles a rock wall) add directly.  The last
-// block gathers the partials (comp_gather), so no address receives an atomic
-// from every block.
-__device__ __forceinline__ void comp_add(const MpArgs& a, double* sums, const Cell& c, float v) {
-  __shared__ int dom;
+// Per-component FP64 sums of a per-cell value.  The block's dominant
+// component is that of its first water cell (smallest position; key =
+// position << 16 | component, components below 2^16); the block sums its
+// cells of that component and records the partial with the component, and
+// cells of other components (rare: the block straddles a rock wall) add
+// directly.  The last block gathers the partials (comp_gather), so no address
+// receives an atomic from every block.
+__device__ __forceinline__ int block_dom(int key) {
+  __shared__ int best;
+  if (threadIdx.x == 0 && threadIdx.y == 0) best = 0x7fffffff;
+  __syncthreads();
+  if (key != 0x7fffffff) atomicMin(&best, key);
+  __syncthreads();
+  const int b = best;
+  return b == 0x7fffffff ? -1 : (b & 0xffff);
+}
+__device__ __forceinline__ void comp_record(const MpArgs& a, double* sums, int dom, const float* v, const int* lab) {
   __shared__ double sh[NT / 32];
   const int tid = threadIdx.y * BX + threadIdx.x;
-  if (tid == 0) {
-    int dm = -1;
-    for (int j = 0; j < BY && dm < 0; j++)
-      for (int i = 0; i < BX && dm < 0; i++) {
-        const int x = blockIdx.x * BX + i, y = blockIdx.y * BY + j;
-        if (x < a.fw && y < a.fh) dm = a.label[(size_t)y * a.fw + x];
-      }
-    dom = dm;
-  }
-  __syncthreads();
   float own = 0.0f;
-  if (c.water) {
-    const int lab = a.label[c.i];
-    if (lab == dom) own = v;
-    else atomicAdd(sums + lab, (double)v);
+#pragma unroll
+  for (int k = 0; k < RR; k++) {
+    if (lab[k] < 0) continue;
+    if (lab[k] == dom) own += v[k];
+    else atomicAdd(sums + lab[k], (double)v[k]);
   }
   double dv = (double)own;
   for (int o = 16; o > 0; o >>= 1) dv += __shfl_down_sync(0xffffffffu, dv, o);
@@ -313,53 +321,64 @@ __global__ void k_mp_begin(MpArgs a, int max_outer, int max_inner, float tol, fl
 // starts from e = 0 on it.  The last block decides both loops.
 __global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphConditionalHandle h_outer,
                                                     cudaGraphConditionalHandle h_inner, int final_pass, int graph) {
-  const Cell c = cell_of(a);
-  float rf = 0.0f, b = 0.0f;
-  if (c.water) {
-    const df32 pi = df32{a.hi[c.i], a.lo[c.i]};
-    df32 s = df32{0.0f, 0.0f};
-    const int nb[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+  float rf[RR];
+  int lab[RR];
+  float rn2 = 0.0f, bn2 = 0.0f;
+  int key = 0x7fffffff;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int x = c.x + nb[k][0], y = c.y + nb[k][1];
-      if (x < 0 || y < 0 || x >= a.fw || y >= a.fh) continue;
-      const size_t j = (size_t)y * a.fw + x;
-      if (!a.fl[j]) continue;
-      s = df_add(s, df_add(df32{a.hi[j], a.lo[j]}, df_neg(pi)));
+  for (int k = 0; k < RR; k++) {
+    const Cell c = cell_at(a, k);
+    rf[k] = 0.0f;
+    lab[k] = -1;
+    if (c.water) {
+      const df32 pi = df32{a.hi[c.i], a.lo[c.i]};
+      df32 s = df32{0.0f, 0.0f};
+      const int nb[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        const int x = c.x + nb[n][0], y = c.y + nb[n][1];
+        if (x < 0 || y < 0 || x >= a.fw || y >= a.fh) continue;
+        const size_t j = (size_t)y * a.fw + x;
+        if (!a.fl[j]) continue;
+        s = df_add(s, df_add(df32{a.hi[j], a.lo[j]}, df_neg(pi)));
+      }
+      const df32 lp = df_add(s, df_neg(df_mul_f(pi, a.eps0)));
+      const float b = a.rhs[c.i];
+      const df32 res = df_add(df32{b, 0.0f}, df_neg(lp));
+      rf[k] = res.hi + res.lo;
+      rn2 += rf[k] * rf[k];
+      bn2 += b * b;
+      lab[k] = a.label[c.i];
+      if (key == 0x7fffffff) key = (cell_pos(k) << 16) | lab[k];
     }
-    const df32 lp = df_add(s, df_neg(df_mul_f(pi, a.eps0)));
-    b = a.rhs[c.i];
-    const df32 res = df_add(df32{b, 0.0f}, df_neg(lp));
-    rf = res.hi + res.lo;
+    if (c.in) {
+      a.r[c.i] = rf[k];
+      a.e[c.i] = 0.0f;
+    }
   }
-  if (c.in) {
-    a.r[c.i] = rf;
-    a.e[c.i] = 0.0f;
-  }
-  if (!final_pass) comp_add(a, a.comp_sum_r, c, rf);
-  if (!block_partials(a, rf * rf, b * b)) return;
-  float rn2, bn2;
-  total_partials(a, rn2, bn2);
+  if (!final_pass) comp_record(a, a.comp_sum_r, block_dom(key), rf, lab);
+  if (!block_partials(a, rn2, bn2)) return;
+  float trn2, tbn2;
+  total_partials(a, trn2, tbn2);
   MpCtl* ctl = a.ctl;
   const int tid = threadIdx.y * BX + threadIdx.x;
   if (final_pass) {
-    for (int k = tid; k < ctl->ncomp; k += NT) a.comp_sum_r[k] = 0.0;
     if (tid == 0) {
-      ctl->rho = ctl->bn2 > 0.0 ? sqrt((double)rn2 / ctl->bn2) : 0.0;
+      ctl->rho = ctl->bn2 > 0.0 ? sqrt((double)trn2 / ctl->bn2) : 0.0;
       ctl->done = 0;
     }
     return;
   }
-  finish_residual_stats(a, rn2);
+  finish_residual_stats(a, trn2);
   if (tid == 0) {
-    if (ctl->outer == 0) ctl->bn2 = (double)bn2;
-    const double rho2 = ctl->bn2 > 0.0 ? (double)rn2 / ctl->bn2 : 0.0;
+    if (ctl->outer == 0) ctl->bn2 = (double)tbn2;
+    const double rho2 = ctl->bn2 > 0.0 ? (double)trn2 / ctl->bn2 : 0.0;
     ctl->rho = sqrt(rho2);
     const bool conv = rho2 <= (double)ctl->tol2 || !(rho2 == rho2);
     ctl->converged = conv ? 1 : 0;
     ctl->inner = 0;
     ctl->inner_done = conv ? 1 : 0;
-    ctl->r0n2 = rn2;
+    ctl->r0n2 = trn2;
     // the inner solve stops at mixed_inner_tol, or as soon as the outer
     // residual would be half the tolerance if it is closer than that
     const double need = rho2 > 0.0 ? 0.25 * (double)ctl->tol2 / rho2 : 1.0;
@@ -373,25 +392,27 @@ __global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphCondition
   }
 }
 
-// z <- z - (mean of z over its component) - comp_mean / eps0, then the dot
-// products z.r and z.q of the flexible CG.
+// z <- z - (mean of z over its component) - comp_mean / eps0 (the shift
+// k_mp_zshift formed), then the dot products z.r and z.q of the flexible CG.
 __global__ void __launch_bounds__(NT) k_mp_dots(MpArgs a) {
-  const Cell c = cell_of(a);
   float zr = 0.0f, zq = 0.0f;
-  if (c.water) {
-    const float zc = a.z[c.i] - a.comp_shift[a.label[c.i]];
-    a.z[c.i] = zc;
-    zr = zc * a.r[c.i];
-    zq = zc * a.q[c.i];
-  } else if (c.in) {
-    a.z[c.i] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < RR; k++) {
+    const Cell c = cell_at(a, k);
+    if (c.water) {
+      const float zc = a.z[c.i] - a.comp_shift[a.label[c.i]];
+      a.z[c.i] = zc;
+      zr += zc * a.r[c.i];
+      zq += zc * a.q[c.i];
+    } else if (c.in) {
+      a.z[c.i] = 0.0f;
+    }
   }
   if (!block_partials(a, zr, zq)) return;
   float tzr, tzq;
   total_partials(a, tzr, tzq);
-  MpCtl* ctl = a.ctl;
-  const int tid = threadIdx.y * BX + threadIdx.x;
-  if (tid == 0) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    MpCtl* ctl = a.ctl;
     ctl->beta = (ctl->inner == 0 || ctl->rz == 0.0f) ? 0.0f : -ctl->alpha * tzq / ctl->rz;
     ctl->rz = tzr;
     ctl->done = 0;
@@ -414,30 +435,35 @@ __global__ void __launch_bounds__(NT) k_mp_zshift(MpArgs a, unsigned ntiles) {
 }
 
 __global__ void __launch_bounds__(NT) k_mp_direction(MpArgs a) {
-  const Cell c = cell_of(a);
-  if (!c.in) return;
   const float beta = a.ctl->beta;
   const bool first = a.ctl->inner == 0;  // d starts as z (whatever d held before)
-  a.d[c.i] = c.water ? (first ? a.z[c.i] : a.z[c.i] + beta * a.d[c.i]) : 0.0f;
+#pragma unroll
+  for (int k = 0; k < RR; k++) {
+    const Cell c = cell_at(a, k);
+    if (c.in) a.d[c.i] = c.water ? (first ? a.z[c.i] : a.z[c.i] + beta * a.d[c.i]) : 0.0f;
+  }
 }
 
 // q = L d in FP32 (differences first, so a constant d gives -eps0 * d
 // exactly), and d.q; alpha = z.r / d.q.
 __global__ void __launch_bounds__(NT) k_mp_matvec(MpArgs a) {
-  const Cell c = cell_of(a);
   float dq = 0.0f;
-  if (c.water) {
-    const float di = a.d[c.i];
-    float s = 0.0f;
-    if (c.x > 0 && a.fl[c.i - 1]) s += a.d[c.i - 1] - di;
-    if (c.x + 1 < a.fw && a.fl[c.i + 1]) s += a.d[c.i + 1] - di;
-    if (c.y > 0 && a.fl[c.i - a.fw]) s += a.d[c.i - a.fw] - di;
-    if (c.y + 1 < a.fh && a.fl[c.i + a.fw]) s += a.d[c.i + a.fw] - di;
-    const float q = s - a.eps0 * di;
-    a.q[c.i] = q;
-    dq = di * q;
-  } else if (c.in) {
-    a.q[c.i] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < RR; k++) {
+    const Cell c = cell_at(a, k);
+    if (c.water) {
+      const float di = a.d[c.i];
+      float s = 0.0f;
+      if (c.x > 0 && a.fl[c.i - 1]) s += a.d[c.i - 1] - di;
+      if (c.x + 1 < a.fw && a.fl[c.i + 1]) s += a.d[c.i + 1] - di;
+      if (c.y > 0 && a.fl[c.i - a.fw]) s += a.d[c.i - a.fw] - di;
+      if (c.y + 1 < a.fh && a.fl[c.i + a.fw]) s += a.d[c.i + a.fw] - di;
+      const float q = s - a.eps0 * di;
+      a.q[c.i] = q;
+      dq += di * q;
+    } else if (c.in) {
+      a.q[c.i] = 0.0f;
+    }
   }
   if (!block_partials(a, dq, 0.0f)) return;
   float tdq, unused;
@@ -452,25 +478,35 @@ __global__ void __launch_bounds__(NT) k_mp_matvec(MpArgs a) {
 // e += alpha d, r -= alpha q; the last block tests the inner tolerance,
 // prepares the next preconditioner input and sets the inner loop condition.
 __global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHandle h_inner, int graph) {
-  const Cell c = cell_of(a);
   const float alpha = a.ctl->alpha;
-  float rn = 0.0f;
-  if (c.water) {
-    a.e[c.i] += alpha * a.d[c.i];
-    rn = a.r[c.i] - alpha * a.q[c.i];
-    a.r[c.i] = rn;
+  float rn[RR];
+  int lab[RR];
+  float rn2 = 0.0f;
+  int key = 0x7fffffff;
+#pragma unroll
+  for (int k = 0; k < RR; k++) {
+    const Cell c = cell_at(a, k);
+    rn[k] = 0.0f;
+    lab[k] = -1;
+    if (c.water) {
+      a.e[c.i] += alpha * a.d[c.i];
+      rn[k] = a.r[c.i] - alpha * a.q[c.i];
+      a.r[c.i] = rn[k];
+      rn2 += rn[k] * rn[k];
+      lab[k] = a.label[c.i];
+      if (key == 0x7fffffff) key = (cell_pos(k) << 16) | lab[k];
+    }
   }
-  comp_add(a, a.comp_sum_r, c, rn);
-  if (!block_partials(a, rn * rn, 0.0f)) return;
-  float rn2, unused;
-  total_partials(a, rn2, unused);
-  finish_residual_stats(a, rn2);
-  const int tid = threadIdx.y * BX + threadIdx.x;
-  if (tid == 0) {
+  comp_record(a, a.comp_sum_r, block_dom(key), rn, lab);
+  if (!block_partials(a, rn2, 0.0f)) return;
+  float trn2, unused;
+  total_partials(a, trn2, unused);
+  finish_residual_stats(a, trn2);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
     MpCtl* ctl = a.ctl;
     ctl->inner += 1;
     ctl->total_inner += 1;
-    const bool done = rn2 <= ctl->itarget2 * ctl->r0n2 || !(rn2 == rn2);
+    const bool done = trn2 <= ctl->itarget2 * ctl->r0n2 || !(trn2 == trn2);
     ctl->inner_done = done ? 1 : 0;
     ctl->done = 0;
     if (graph) cudaGraphSetConditional(h_inner, (!done && ctl->inner < ctl->max_inner) ? 1u : 0u);
@@ -479,16 +515,19 @@ __global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHa
 
 // (hi, lo) += e; walls hold 0 (as the f32 multigrid leaves them).
 __global__ void __launch_bounds__(NT) k_mp_update(MpArgs a) {
-  const Cell c = cell_of(a);
-  if (!c.in) return;
-  if (!c.water) {
-    a.hi[c.i] = 0.0f;
-    a.lo[c.i] = 0.0f;
-    return;
+#pragma unroll
+  for (int k = 0; k < RR; k++) {
+    const Cell c = cell_at(a, k);
+    if (!c.in) continue;
+    if (!c.water) {
+      a.hi[c.i] = 0.0f;
+      a.lo[c.i] = 0.0f;
+      continue;
+    }
+    const df32 p = df_add(df32{a.hi[c.i], a.lo[c.i]}, df32{a.e[c.i], 0.0f});
+    a.hi[c.i] = p.hi;
+    a.lo[c.i] = p.lo;
   }
-  const df32 p = df_add(df32{a.hi[c.i], a.lo[c.i]}, df32{a.e[c.i], 0.0f});
-  a.hi[c.i] = p.hi;
-  a.lo[c.i] = p.lo;
 }
 
 }  // namespace
@@ -562,7 +601,7 @@ int setting_or(uint32_t v, int dflt) { return v > 0 ? (int)v : dflt; }
 // loop and the update.
 cudaError_t capture_solve(World& w, MixedSolver& m, cudaStream_t s) {
   const MpArgs a = mp_args(w, m);
-  const dim3 grid((w.fw + BX - 1) / BX, (w.fh + BY - 1) / BY), blk(BX, BY);
+  const dim3 grid((w.fw + BX - 1) / BX, (w.fh + BY * RR - 1) / (BY * RR)), blk(BX, BY);
   const ribo_world_settings& st = w.st;
   cudaStreamCaptureStatus cs;
   unsigned long long id = 0;
@@ -638,7 +677,7 @@ cudaError_t capture_solve(World& w, MixedSolver& m, cudaStream_t s) {
 cudaError_t direct_solve(World& w, MixedSolver& m) {
   const MpArgs a = mp_args(w, m);
   cudaStream_t s = w.stream;
-  const dim3 grid((w.fw + BX - 1) / BX, (w.fh + BY - 1) / BY), blk(BX, BY);
+  const dim3 grid((w.fw + BX - 1) / BX, (w.fh + BY * RR - 1) / (BY * RR)), blk(BX, BY);
   const ribo_world_settings& st = w.st;
   const int max_outer = setting_or(st.mixed_max_outer, 4), max_inner = setting_or(st.mixed_max_inner, 64);
   const double F = (double)w.fcells();
