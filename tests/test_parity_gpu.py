@@ -63,6 +63,23 @@ def test_steps_bit_exact(rw, ro, case):
     assert g.ledger_blocking() == o.ledger_blocking()
 
 
+def test_c0_hundred_steps_bit_exact(rw, ro):
+    """The c0 configuration in full: 256^2, multigrid 5 levels to 16x16, 2
+    V-cycles of 3+3 sweeps, every step a fluid + transport step, 100 steps;
+    counts and every field bit-exact with the oracle (checked along the way
+    and at the end)."""
+    g, o, _ = setup_pair(rw, ro, 256, params=BASE, settings=dict(fluid_substep=1, mg_cycles=2),
+                         mg_min_size=16, mg_pre=3, mg_post=3)
+    done = 0
+    for batch in (50, 50):
+        g.encode_steps(batch)
+        o.encode_steps(batch)
+        done += batch
+        compare_worlds(g, o, f"c0 after {done} steps")
+    assert done == 100
+    assert g.ledger_blocking() == o.ledger_blocking()
+
+
 def test_graph_replay_matches_direct_launches(rw, ro):
     """Repeated step sequences replay from CUDA graphs; the results must equal
     direct launches and the oracle."""
