@@ -146,8 +146,10 @@ __device__ __forceinline__ uint4 load_cell(const uint32_t* chem, size_t idx) {
   return __ldg(reinterpret_cast<const uint4*>(chem) + idx);
 }
 
-// fluid.wgsl:62-64
+// fluid.wgsl:62-64.  With the surface temperature 0 the product is +0 for
+// every cell (the exponential is finite and positive), so it is not evaluated.
 __device__ __forceinline__ float temp_ambient_at(const Dev& d, uint32_t y) {
+  if (TEMP_AMBIENT_SURFACE == 0.0f) return 0.0f;
   return TEMP_AMBIENT_SURFACE * rb_exp(-TEMP_AMBIENT_ATTEN * (1.0f - ((float)y + 0.5f) / (float)d.fh));
 }
 // fluid.wgsl:46-54
