@@ -70,8 +70,11 @@ __global__ void k_temperature(const __grid_constant__ S s) {
   float tl = T[(size_t)y * fw + xl], tr = T[(size_t)y * fw + xr], tb = T[(size_t)yb * fw + x], tt = T[(size_t)yt * fw + x];
   float fill = gamma_fill_at_fluid_cell(d, x, y);
   t = rb_mix(t, (tl + tr + tb + tt) * 0.25f, TEMP_DIFFUSE * rb_mix(1.0f, TEMP_ROCK_CONDUCT, fill));
-  float vc = vent_cycle(d, P, x);
-  float2 h = d.heat[idx];
+  const float2 h = d.heat[idx];
+  // The vent cycle only scales vent heat.  It is finite and >= +0 for a
+  // finite amplitude, so with no heat here both products are zeros of the
+  // heat's signs whatever its value, and the sine is not evaluated.
+  const float vc = (h.x != 0.0f || h.y != 0.0f || !(P->vent_cycle_amp <= 3.0e38f)) ? vent_cycle(d, P, x) : 1.0f;
   t += h.x * vc * TEMP_HEAT_RATE * dt;
   if (rb_max(P->sun_heat, 0.0f) > 0.0f) {  // otherwise the sun term is exactly 0
     size_t env = env_cell_for_fluid(d, x, y);
@@ -80,7 +83,10 @@ __global__ void k_temperature(const __grid_constant__ S s) {
     t += rb_max(P->sun_heat, 0.0f) * SUN_HEAT_RATE * (light_absorbed_at(d, P, env) + ir) * dt;
   }
   float amb = temp_ambient_at(d, y);
-  t = amb + (t - amb) * rb_exp(-TEMP_COOL_RATE * (1.0f - fill) * dt);
+  // dt is finite in [0, MAX_DT] and fill in [0, 1], so the cooling factor is
+  // finite; with the ambient +0 a zero temperature stays +0 without it.
+  if (TEMP_AMBIENT_SURFACE == 0.0f && t == 0.0f) t = 0.0f;
+  else t = amb + (t - amb) * rb_exp(-TEMP_COOL_RATE * (1.0f - fill) * dt);
   d.temp_out[idx] = rb_clamp(t, 0.0f, TEMP_MAX);
 
   const float* R = d.redox_in;
@@ -90,7 +96,9 @@ __global__ void k_temperature(const __grid_constant__ S s) {
   r = rb_mix(r, (rl + rr + rbt + rt) * 0.25f, TEMP_DIFFUSE);
   r += h.y * vc * REDOX_RATE * dt;
   r = rb_max(r - (float)d.redox_eaten[idx] / REDOX_FP, 0.0f);
-  r *= rb_exp(-rb_max(P->redox_decay, 0.0f) * dt);
+  // a zero times a finite factor in [0, 1] keeps its sign: skip the exponential
+  const float decay_arg = -rb_max(P->redox_decay, 0.0f) * dt;
+  if (r != 0.0f || !(decay_arg <= 0.0f)) r *= rb_exp(decay_arg);
   d.redox_out[idx] = rb_clamp(r, 0.0f, REDOX_MAX);
   d.redox_eaten[idx] = 0u;
 }

@@ -333,20 +333,63 @@ constexpr int TX = SCATTER_TX, TY = SCATTER_TY, NT = TX * TY;
 constexpr int HALO = 2, AW = TX + 2 * HALO, AH = TY + 2 * HALO, AC = AW * AH;
 constexpr uint16_t FAR = 0xFFFFu;  // destination outside the accumulator
 
+// Per (cell, channel) word of the mover loop: bits 0-8 the activated count
+// after the local reactions, capped at 511 (a mover index k is below
+// MAX_MOVERS_PER_CH <= 511, so k < act_n reads the same); bits 9-24 the
+// activated counts m of the four neighbours in this channel, each capped at
+// 8 (4 bits; 15 where the neighbour is off the grid), which select the
+// cohesion factor cohf[m] = 1 + cohesion * m of an activated monomer's hop
+// weights (cohf is 1 for m = 15 and wherever cohesion is off).
+constexpr uint32_t ACT_BITS = 9, ACT_MASK = (1u << ACT_BITS) - 1u;
+static_assert(MAX_MOVERS_PER_CH <= ACT_MASK, "mover index must fit the activated-count field");
+
 struct Smem {
   // per cell (index = warp * 32 + lane)
-  float dispx[NT], dispy[NT];
-  int basex[NT], basey[NT];
-  float p_diff[NT], p_settle[NT], p_bound[NT], bsx[NT], bsy[NT], dlen[NT];
-  float press[4][NT], acc[4][NT], accs[4][NT];
-  uint32_t actn[4][NT];            // activated after the local reactions, per channel
+  float4 mv0[NT];                  // displacement x, y; p_diff; p_diff + p_settle
+  float4 mv1[NT];                  // p_bound; bound start x, y; dispersion length (or -1)
+  float4 press[NT];                // osmotic hop weights (+x, -x, +y, -y)
+  float acc[8][NT];                // Kawasaki acceptance per direction: activated 0-3, spent 4-7
+  uint32_t segw[4][NT];            // per channel: activated count | neighbour counts (above)
   uint16_t slot[16][NT];           // accumulator slot of each window bin (blocking resolved), or FAR
   uint32_t off[TY][4 * TX + 1];    // per warp: exclusive prefix of movers over (cell, channel)
   uint32_t accum[AC][4];           // tile + ring destination sums [cell][channel]
   uint8_t rock[AC], full[AC];
+  float cohf[16];                  // 1 + cohesion * m for m = 0..8 (1 where cohesion is off)
   float2 lattice[4][4];            // smooth_start lattice values of this tile
   float2 jit, glob;                // smooth_start per-step jitter and offset
 };
+
+// rb_pcg4d(a, b, c, d) split at the first word that varies inside a mover
+// loop: `head` carries the part fixed by (a, b, d), `draw` finishes the hash
+// for c.  Same integer operations in the same order, so the same bits.
+struct PcgHead {
+  uint32_t x1, y0, w0;
+};
+__device__ __forceinline__ PcgHead pcg_head(uint32_t a, uint32_t b, uint32_t dd) {
+  PcgHead h;
+  h.y0 = b * 1664525u + 1013904223u;
+  h.w0 = dd * 1664525u + 1013904223u;
+  h.x1 = (a * 1664525u + 1013904223u) + h.y0 * h.w0;
+  return h;
+}
+// z0 = c * 1664525 + 1013904223 (the caller steps it by 1664525 per c)
+__device__ __forceinline__ rb_u4 pcg_draw(const PcgHead& h, uint32_t z0) {
+  uint32_t x = h.x1;
+  uint32_t y = h.y0 + z0 * x;
+  uint32_t z = z0 + x * y;
+  uint32_t w = h.w0 + y * z;
+  x ^= x >> 16;
+  y ^= y >> 16;
+  z ^= z >> 16;
+  w ^= w >> 16;
+  x += y * w;
+  y += z * x;
+  z += x * y;
+  w += y * z;
+  rb_u4 r = {x, y, z, w};
+  return r;
+}
+constexpr uint32_t pcg_z0(uint32_t c) { return c * 1664525u + 1013904223u; }
 }  // namespace st
 
 template <class Sel>
@@ -387,6 +430,9 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
     uint32_t ix = lgx0 + (tid & 3), iy = lgy0 + (tid >> 2);
     rb_u4 r = rb_pcg4d((ix * 73856093u) ^ (iy * 19349663u), P->epoch, RB_S_MOVE + MAX_MOVERS_PER_CH + 1u, P->seed);
     S.lattice[tid >> 2][tid & 3] = f2(rb_u2f(r.x), rb_u2f(r.y));
+  } else if (tid >= 32 && tid < 48) {
+    const int m = tid - 32;
+    S.cohf[m] = P->cohesion > 0.0f && m <= 8 ? 1.0f + P->cohesion * (float)m : 1.0f;
   }
   __syncthreads();
 
@@ -430,17 +476,36 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       if (g_src == 0u) p_settle = rb_min(MONOMER_SETTLE_P * rb_max(P->settle, 0.0f) * tn, 0.5f);
       float press[4] = {1.0f, 1.0f, 1.0f, 1.0f};
       float max_drop = 0.0f;
-      if (P->monomer_pressure > 0.0f) {
-        float f_self = (float)src_total / (float)(cap_self > 1u ? cap_self : 1u);
-        long nb[4] = {1, -1, (long)G, -(long)G};
-        bool inside[4] = {x + 1u < G, x > 0u, y + 1u < GH, y > 0u};
+      // neighbour counts for the cohesion factors, 4 bits per direction and
+      // channel (transport.wgsl:298-304 reads the same words per monomer);
+      // 15 marks a neighbour off the grid, whose factor is 1
+      uint32_t nbm[4] = {0u, 0u, 0u, 0u};
+      const bool use_press = P->monomer_pressure > 0.0f, use_coh = P->cohesion > 0.0f;
+      if (use_press || use_coh) {
+        const float f_self = (float)src_total / (float)(cap_self > 1u ? cap_self : 1u);
+        const long nb[4] = {1, -1, (long)G, -(long)G};
+        const bool inside[4] = {x + 1u < G, x > 0u, y + 1u < GH, y > 0u};
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-          if (!inside[k]) continue;
-          size_t n = (size_t)((long)idx + nb[k]);
-          uint32_t cap_n = capacity_of(__ldg(d.gamma + n));
+          if (!inside[k]) {
+            nbm[0] |= 15u << (4 * k);
+            nbm[1] |= 15u << (4 * k);
+            nbm[2] |= 15u << (4 * k);
+            nbm[3] |= 15u << (4 * k);
+            continue;
+          }
+          const size_t n = (size_t)((long)idx + nb[k]);
+          const uint4 wn = load_cell(d.chem, n);
+          if (use_coh) {
+            nbm[0] |= umin(wn.x & CHEM_STATE_MASK, 8u) << (4 * k);
+            nbm[1] |= umin(wn.y & CHEM_STATE_MASK, 8u) << (4 * k);
+            nbm[2] |= umin(wn.z & CHEM_STATE_MASK, 8u) << (4 * k);
+            nbm[3] |= umin(wn.w & CHEM_STATE_MASK, 8u) << (4 * k);
+          }
+          if (!use_press) continue;
+          const uint32_t cap_n = capacity_of(__ldg(d.gamma + n));
           if (cap_n == 0u) continue;
-          float f_n = (float)cell_total4(load_cell(d.chem, n)) / (float)cap_n;
+          const float f_n = (float)cell_total4(wn) / (float)cap_n;
           press[k] = rb_max((float)0.05, 1.0f + P->monomer_pressure * (f_self - f_n));
           max_drop = rb_max(max_drop, f_self - f_n);
         }
@@ -482,21 +547,13 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       }
       const bool disperse = g_src > 0u && (disp.x != 0.0f || disp.y != 0.0f);
       const int basex = rb_floor_i(disp.x) - 1, basey = rb_floor_i(disp.y) - 1;
-      S.dispx[tid] = disp.x;
-      S.dispy[tid] = disp.y;
-      S.basex[tid] = basex;
-      S.basey[tid] = basey;
-      S.p_diff[tid] = p_diff;
-      S.p_settle[tid] = p_settle;
-      S.p_bound[tid] = p_bound;
-      S.bsx[tid] = bound_start.x;
-      S.bsy[tid] = bound_start.y;
-      S.dlen[tid] = disperse ? len2(disp) : -1.0f;
+      S.mv0[tid] = make_float4(disp.x, disp.y, p_diff, p_diff + p_settle);
+      S.mv1[tid] = make_float4(p_bound, bound_start.x, bound_start.y, disperse ? len2(disp) : -1.0f);
+      S.press[tid] = make_float4(press[0], press[1], press[2], press[3]);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        S.press[k][tid] = press[k];
         S.acc[k][tid] = acc[k];
-        S.accs[k][tid] = accs[k];
+        S.acc[4 + k][tid] = accs[k];
       }
       // destination slot of every window bin (transport.wgsl:364-401)
 #pragma unroll 4
@@ -531,7 +588,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         const uint32_t slot = (uint32_t)(idx * 4 + ch);
         uint32_t act_n = words[ch] & CHEM_STATE_MASK;
         uint32_t spent_n = words[ch] >> 16;
-        S.actn[ch][tid] = 0u;
+        S.segw[ch][tid] = 0u;
         if (act_n + spent_n == 0u) continue;
         if (spent_n > 0u) {
           float sens = 1.0f + CHEM_SENSITIZE * (float)umin(act_n, 8u);
@@ -558,7 +615,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         const uint32_t act_stay = act_n - umin(act_n, movers);
         const uint32_t stay = act_stay + (n - movers - act_stay) * CHEM_SPENT_ONE;
         if (stay) atomicAdd(&S.accum[say * st::AW + sax][ch], stay);
-        S.actn[ch][tid] = act_n;
+        S.segw[ch][tid] = umin(act_n, st::ACT_MASK) | (act_n > 0u ? nbm[ch] << st::ACT_BITS : 0u);
         mov[ch] = movers;
       }
     }
@@ -602,76 +659,71 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
     int ct = warp * 32 + c;
     const int cy = Y0 + warp;
     int cx = X0 + c;
-    uint32_t slot = (uint32_t)(((size_t)cy * G + cx) * 4 + ch);
-    uint32_t act_n = S.actn[ch][ct];
-    float dispx = S.dispx[ct], dispy = S.dispy[ct], p_diff = S.p_diff[ct], p_settle = S.p_settle[ct];
-    float p_bound = S.p_bound[ct], bsx = S.bsx[ct], bsy = S.bsy[ct], dlen = S.dlen[ct];
-    int basex = S.basex[ct], basey = S.basey[ct];
     const uint32_t epoch = P->epoch, seed = P->seed;
-    const float cohesion = P->cohesion;
-    for (; j < j_end; j++) {
-      if (j >= seg_end) {  // next non-empty segment
+    // per segment: the hash head of its slot, the cell's mover parameters
+    st::PcgHead ph = st::pcg_head((uint32_t)(((size_t)cy * G + cx) * 4 + ch), epoch, seed);
+    uint32_t segw = S.segw[ch][ct];
+    float4 mv0 = S.mv0[ct], mv1 = S.mv1[ct];
+    int basex = rb_floor_i(mv0.x) - 1, basey = rb_floor_i(mv0.y) - 1;
+    // z word of the move draw for mover k (stepped with k below)
+    uint32_t zk = st::pcg_z0(RB_S_MOVE + k);
+    constexpr uint32_t Z_DISPERSE = st::pcg_z0(RB_S_DISPERSE) - st::pcg_z0(RB_S_MOVE);
+    for (; j < j_end; j++, k++, zk += 1664525u) {
+      if (j >= seg_end) {  // next non-empty segment; it starts at mover 0
         do {
           s++;
           seg_end = off[s + 1];
         } while (j >= seg_end);
-        k = j - off[s];
+        k = 0u;
+        zk = st::pcg_z0(RB_S_MOVE);
         c = s >> 2;
         ch = s & 3;
         ct = warp * 32 + c;
         cx = X0 + c;
-        slot = (uint32_t)(((size_t)cy * G + cx) * 4 + ch);
-        act_n = S.actn[ch][ct];
-        dispx = S.dispx[ct];
-        dispy = S.dispy[ct];
-        p_diff = S.p_diff[ct];
-        p_settle = S.p_settle[ct];
-        p_bound = S.p_bound[ct];
-        bsx = S.bsx[ct];
-        bsy = S.bsy[ct];
-        dlen = S.dlen[ct];
-        basex = S.basex[ct];
-        basey = S.basey[ct];
+        ph = st::pcg_head((uint32_t)(((size_t)cy * G + cx) * 4 + ch), epoch, seed);
+        segw = S.segw[ch][ct];
+        mv0 = S.mv0[ct];
+        mv1 = S.mv1[ct];
+        basex = rb_floor_i(mv0.x) - 1;
+        basey = rb_floor_i(mv0.y) - 1;
       }
-      const bool is_act = k < act_n;
+      const bool is_act = k < (segw & st::ACT_MASK);
       const uint32_t unit = is_act ? 1u : CHEM_SPENT_ONE;
-      rb_u4 ru = rb_pcg4d(slot, epoch, RB_S_MOVE + k, seed);
-      float rfx = rb_u2f(ru.x), rfy = rb_u2f(ru.y), rfz = rb_u2f(ru.z), rfw = rb_u2f(ru.w);
-      bool bound = is_act && p_bound > 0.0f && rb_fract(rfz * (float)7.31 + rfw * (float)3.17) < p_bound;
-      float px = (bound ? bsx : rfx) + dispx;
-      float py = (bound ? bsy : rfy) + dispy;
+      const rb_u4 ru = st::pcg_draw(ph, zk);  // rb_pcg4d(slot, epoch, RB_S_MOVE + k, seed)
+      const float rfx = rb_u2f(ru.x), rfy = rb_u2f(ru.y), rfz = rb_u2f(ru.z), rfw = rb_u2f(ru.w);
+      const float p_bound = mv1.x, dlen = mv1.w;
+      const bool bound = is_act && p_bound > 0.0f && rb_fract(rfz * (float)7.31 + rfw * (float)3.17) < p_bound;
+      float px = (bound ? mv1.y : rfx) + mv0.x;
+      float py = (bound ? mv1.z : rfy) + mv0.y;
       if (dlen >= 0.0f) {
-        rb_u4 rj = rb_pcg4d(slot, epoch, RB_S_DISPERSE + k, seed);
+        const rb_u4 rj = st::pcg_draw(ph, zk + Z_DISPERSE);  // rb_pcg4d(slot, epoch, RB_S_DISPERSE + k, seed)
         float jxx = (rb_u2f(rj.x) * 2.0f - 1.0f) * dlen * RUBBLE_DISPERSION;
         float jyy = (rb_u2f(rj.y) * 2.0f - 1.0f) * dlen * RUBBLE_DISPERSION;
         px += rb_clamp(jxx, (float)-0.9, (float)0.9);
         py += rb_clamp(jyy, (float)-0.9, (float)0.9);
       }
-      if (rfz < p_diff) {
-        float w0 = S.press[0][ct], w1 = S.press[1][ct], w2 = S.press[2][ct], w3 = S.press[3][ct];
-        if (is_act && cohesion > 0.0f) {
-          // cohesion weights (transport.wgsl:298-304), only needed on a hop
-          const size_t ci = (size_t)cy * G + cx;
-          if ((uint32_t)cx + 1u < G) w0 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci + 1) * 4 + ch) & CHEM_STATE_MASK, 8u);
-          if (cx > 0) w1 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci - 1) * 4 + ch) & CHEM_STATE_MASK, 8u);
-          if ((uint32_t)cy + 1u < GH) w2 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci + G) * 4 + ch) & CHEM_STATE_MASK, 8u);
-          if (cy > 0) w3 *= 1.0f + cohesion * (float)umin(__ldg(d.chem + (ci - G) * 4 + ch) & CHEM_STATE_MASK, 8u);
-        }
+      if (rfz < mv0.z) {
+        // hop weights: osmotic pressure times, for an activated monomer, the
+        // cohesion factors (transport.wgsl:298-304)
+        const float4 pr = S.press[ct];
+        const uint32_t mw = is_act ? segw >> st::ACT_BITS : 0xFFFFu;
+        const float w0 = pr.x * S.cohf[mw & 15u], w1 = pr.y * S.cohf[(mw >> 4) & 15u];
+        const float w2 = pr.z * S.cohf[(mw >> 8) & 15u], w3 = pr.w * S.cohf[mw >> 12];
         float u = rfw * (w0 + w1 + w2 + w3);
         uint32_t dd;
         if (u < w0) dd = 0u;
         else if ((u -= w0) < w1) dd = 1u;
         else if ((u -= w1) < w2) dd = 2u;
         else dd = 3u;
-        float acc_d = is_act ? S.acc[dd][ct] : S.accs[dd][ct];
-        bool stay_put = rb_fract(rfw * (float)13.73 + rfx * (float)5.31) >= acc_d;
+        const float acc_d = S.acc[(is_act ? 0u : 4u) + dd][ct];
+        const bool stay_put = rb_fract(rfw * (float)13.73 + rfx * (float)5.31) >= acc_d;
         if (!stay_put) {
           if (dd == 0u) px += 1.0f;
           else if (dd == 1u) px -= 1.0f;
           else if (dd == 2u) py += 1.0f;
           else py -= 1.0f;
         }
-      } else if (rfz < p_diff + p_settle) {
+      } else if (rfz < mv0.w) {
         py -= 1.0f;
       }
       const int offx = rb_floor_i(px) - basex, offy = rb_floor_i(py) - basey;
@@ -684,7 +736,6 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         int ty = iclamp(cy + basey + (int)(bi >> 2), 0, (int)GH - 1);
         atomicAdd(d.chem_next + ((size_t)ty * G + tx) * 4 + ch, unit);
       }
-      k++;
     }
   }
   __syncthreads();
