@@ -325,9 +325,7 @@ void Batch::plan_mg(Group* g) {
   for (int m : g->members) {
     World& w = *worlds[m];
     if (!multigrid_fused_ok(w.levels.data(), (int)w.levels.size(), c)) return;
-    MgBufs b = w.mg;
-    b.maps = nullptr;
-    mw.push_back(MgWorld{w.dev(), w.levels.data(), (int)w.levels.size(), b});
+    mw.push_back(MgWorld{w.dev(), w.levels.data(), (int)w.levels.size(), w.mg});
   }
   if (capturing) {
     table_error = true;
@@ -592,9 +590,7 @@ ribo_status Batch::autotune(uint32_t* modes_out) {
   for (World* w : worlds) {
     if (w->cfg.mg_pre != w0.cfg.mg_pre || w->cfg.mg_post != w0.cfg.mg_post) continue;
     if (!multigrid_fused_ok(w->levels.data(), (int)w->levels.size(), c)) continue;
-    MgBufs b = w->mg;
-    b.maps = nullptr;
-    mw.push_back(MgWorld{w->dev(), w->levels.data(), (int)w->levels.size(), b});
+    mw.push_back(MgWorld{w->dev(), w->levels.data(), (int)w->levels.size(), w->mg});
   }
   if (mw.empty()) return RIBO_OK;
   MgBatchPlan* probe = multigrid_batch_plan(mw.data(), (int)mw.size(), c, nullptr, 0, stream);

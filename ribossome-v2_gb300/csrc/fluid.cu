@@ -376,65 +376,84 @@ __global__ void k_subtract_gradient(const __grid_constant__ S s, int dir) {
 // f32; the order of those adds fixes the rounding, so each line is summed
 // by one lane in index order.  A block owns 32 lines: its warps 1..7 stream
 // chunks of NF_C elements of those lines into a double-buffered shared
-// tile with coalesced loads, while warp 0 (lane = line) runs the 32 serial
-// add chains over the previous chunk.  Row blocks and column blocks share
-// one launch.
+// tile, while warp 0 (lane = line) runs the 32 serial add chains over the
+// previous chunk.  A chunk is NF_C units of one coalesced warp load (32
+// cells of a row, or one position of the 32 columns); a loader warp issues
+// all its units' loads before storing any, so a chunk costs about one load
+// latency.  Wall cells are stored as +0.0: the running sum starts at +0.0
+// and never becomes -0.0 in round-to-nearest, so adding +0.0 leaves it
+// unchanged, and the chain needs no branch; the water cells are counted
+// separately (the reference's n, an exact integer in f32).  Row blocks and
+// column blocks share one launch.
 constexpr int NF_L = NET_FLUX_LINES, NF_C = 128, NF_THREADS = 256;
+constexpr int NF_LOADERS = NF_THREADS / 32 - 1, NF_UPW = (NF_C + NF_LOADERS - 1) / NF_LOADERS;
+static_assert(NF_L == 32 && NF_C % 32 == 0, "a unit is one warp load");
 template <class S>
 __global__ void __launch_bounds__(NF_THREADS) k_net_flux(const __grid_constant__ S s, int dir) {
   RB_WORLD(s);
   const float2* __restrict__ vin = dir ? d.vb : d.va;
+  const uint8_t* __restrict__ mask = d.mask;
   const int row_blocks = (d.fh + NF_L - 1) / NF_L;
   __shared__ float val[2][NF_L][NF_C + 1];
-  __shared__ uint8_t wall[2][NF_L][NF_C + 4];
+  __shared__ uint32_t wet_cells[NF_L];
   const bool rows = (int)cta.bx < row_blocks;
   const int line0 = (rows ? (int)cta.bx : (int)cta.bx - row_blocks) * NF_L;
   const int nlines = rows ? d.fh : d.fw;
   const int len = rows ? d.fw : d.fh;
   const int nchunks = (len + NF_C - 1) / NF_C;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < NF_L) wet_cells[threadIdx.x] = 0u;
+  uint32_t my_wet = 0;  // column blocks: water cells of line `lane` seen by this loader
 
-  auto load = [&](int c, int b, int t, int nt) {
+  // unit u of a row block: line u / (NF_C / 32), cells 32 (u % (NF_C / 32)) + lane
+  // of the chunk; of a column block: position u of line `lane`
+  auto load = [&](int c, int b, int lw) {
     const int k0 = c * NF_C;
-    for (int e = t; e < NF_L * NF_C; e += nt) {
-      int l, k;
+    float v[NF_UPW];
+    bool wet[NF_UPW];
+#pragma unroll
+    for (int q = 0; q < NF_UPW; q++) {
+      const int u = lw + NF_LOADERS * q;
+      const int l = rows ? u / (NF_C / 32) : lane, k = rows ? (u % (NF_C / 32)) * 32 + lane : u;
+      const int line = line0 + l, pos = k0 + k;
+      const bool in = u < NF_C && line < nlines && pos < len;
+      const size_t i = in ? (rows ? (size_t)line * d.fw + pos : (size_t)pos * d.fw + line) : 0;
+      const float2 sv = sanitize(vin[i]);
+      wet[q] = in && !mask[i];
+      v[q] = rows ? sv.y : sv.x;
+    }
+#pragma unroll
+    for (int q = 0; q < NF_UPW; q++) {
+      const int u = lw + NF_LOADERS * q;
+      if (u >= NF_C) continue;  // uniform over the warp
+      const int l = rows ? u / (NF_C / 32) : lane, k = rows ? (u % (NF_C / 32)) * 32 + lane : u;
+      val[b][l][k] = wet[q] ? v[q] : 0.0f;
       if (rows) {
-        l = e / NF_C;
-        k = e % NF_C;
+        const uint32_t m = __ballot_sync(0xffffffffu, wet[q]);
+        if (lane == 0 && m) atomicAdd(&wet_cells[l], (uint32_t)__popc(m));
       } else {
-        l = e % NF_L;
-        k = e / NF_L;
+        my_wet += wet[q] ? 1u : 0u;
       }
-      int line = line0 + l, pos = k0 + k;
-      float v = 0.0f;
-      uint8_t w = 1;
-      if (line < nlines && pos < len) {
-        size_t i = rows ? (size_t)line * d.fw + pos : (size_t)pos * d.fw + line;
-        w = d.mask[i];
-        float2 s = sanitize(vin[i]);
-        v = rows ? s.y : s.x;
-      }
-      val[b][l][k] = v;
-      wall[b][l][k] = w;
     }
   };
 
-  load(0, 0, threadIdx.x, NF_THREADS);
   __syncthreads();
-  float sum = 0.0f, n = 0.0f;
+  if (warp > 0) load(0, 0, warp - 1);
+  __syncthreads();
+  float sum = 0.0f;
   for (int c = 0; c < nchunks; c++) {
     const int b = c & 1;
     if (warp == 0) {
-      for (int k = 0; k < NF_C; k++) {
-        if (wall[b][lane][k]) continue;
-        sum += val[b][lane][k];
-        n += 1.0f;
-      }
+#pragma unroll 16
+      for (int k = 0; k < NF_C; k++) sum += val[b][lane][k];
     } else if (c + 1 < nchunks) {
-      load(c + 1, b ^ 1, threadIdx.x - 32, NF_THREADS - 32);
+      load(c + 1, b ^ 1, warp - 1);
     }
     __syncthreads();
   }
+  if (!rows && warp > 0 && my_wet) atomicAdd(&wet_cells[lane], my_wet);
+  __syncthreads();
+  const float n = (float)wet_cells[lane];
   if (warp == 0 && line0 + lane < nlines) d.net_flux[(rows ? 0 : d.fh) + line0 + lane] = n > 0.0f ? sum / n : 0.0f;
 }
 

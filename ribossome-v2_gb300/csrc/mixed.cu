@@ -559,6 +559,15 @@ int half_levels(const World& w) {
   return k < HALF_LEVELS ? k : HALF_LEVELS;
 }
 
+// Entries of part_c / part_dom: written per residual block by the CG
+// kernels and per level-0 tile by the V-cycle.
+size_t part_entries(const ribo_world_cfg& c, const std::vector<MgLevel>& levels) {
+  const size_t blocks = ((size_t)(c.fluid_w + BX - 1) / BX) * ((c.fluid_h + BY - 1) / BY);
+  const MgConfig mc{(int)c.mg_pre, (int)c.mg_post, (int)c.mg_coarse, 1};
+  const size_t tiles = mixed_vcycle_tiles(levels.data(), (int)levels.size(), mc);
+  return blocks > tiles ? blocks : tiles;
+}
+
 MpArgs mp_args(const World& w, const MixedSolver& m) {
   MpArgs a{};
   a.fw = w.fw;
@@ -749,8 +758,9 @@ ribo_status mixed_init(World& w) {
   MP_ALLOC(m->comp_size, COMP_CAP * 8);
   MP_ALLOC(m->comp_mean_f, COMP_CAP * 4);
   MP_ALLOC(m->comp_shift, COMP_CAP * 4);
-  MP_ALLOC(m->part_c, blocks * 8);
-  MP_ALLOC(m->part_dom, blocks * 4);
+  const size_t tiles = part_entries(w.cfg, w.levels);
+  MP_ALLOC(m->part_c, tiles * 8);
+  MP_ALLOC(m->part_dom, tiles * 4);
   m->coarsest_cells = last.nx * last.ny;
   MP_ALLOC(m->inv, (size_t)m->coarsest_cells * m->coarsest_cells * 8);
   const int nh = half_levels(w);
@@ -788,7 +798,8 @@ size_t mixed_footprint(const ribo_world_cfg& c, const std::vector<MgLevel>& leve
   const int nl = (int)levels.size();
   const int k = multigrid_first_coarse_level(levels.data(), nl);
   const size_t nc = (size_t)levels[nl - 1].nx * levels[nl - 1].ny;
-  size_t b = F * 4 * 7 + blocks * (8 + 8 + 4) + sizeof(MpCtl) + (size_t)COMP_CAP * (8 * 4 + 4 * 2) + nc * nc * 8;
+  size_t b = F * 4 * 7 + blocks * 8 + part_entries(c, levels) * (8 + 4) + sizeof(MpCtl) + (size_t)COMP_CAP * (8 * 4 + 4 * 2) +
+             nc * nc * 8;
   const int nh = k < HALF_LEVELS ? k : HALF_LEVELS;
   for (int l = 0; l < k; l++) {
     const size_t n = (size_t)levels[l].nx * levels[l].ny, es = l < nh ? 2 : 4;

@@ -13,7 +13,6 @@
 
 #include "ribo_dev.cuh"
 #include "ribo_launch.h"
-#include "ribo_tma.cuh"
 
 namespace ribo {
 
@@ -135,18 +134,27 @@ __global__ void k_jacobi(const __grid_constant__ Dev d, const float* __restrict_
 // Fused V-cycle.
 //
 // Fine levels: one kernel does "pre-smooth nu sweeps + residual + restrict"
-// and one does "prolong + post-smooth nu sweeps", each on a TWxTH tile held
-// in shared memory with a halo of 2nu+1 (resp. 2nu) cells.  Half-sweep s only
-// needs the cells at distance >= s from the loaded region's edge to be
-// exact, so after 2nu half-sweeps the tile interior and its one-cell ring
-// hold exactly the values a dispatch per half-sweep would give.
+// and one does "prolong + post-smooth nu sweeps", each on a tile held in
+// shared memory with a halo of H = 2nu+1 (resp. 2nu) cells: the box.  After
+// half-sweep s the cells at distance > s from the edge of the box hold
+// exactly the values a dispatch per half-sweep would give, whatever the cells
+// nearer the edge hold, so after 2nu half-sweeps the tile and its one-cell
+// ring are exact.  Every half-sweep therefore updates all cells at distance
+// >= 1 (the extra updates near the edge are wasted but keep every lane of a
+// warp on a full row).
 //
-// The tile is staged as a BOXW-wide box starting BOXX cells left of the tile
-// (so its first x coordinate is 16-element aligned, as TMA requires) and H
-// rows above it; TMA copies p, rhs and the water flags in one transaction
-// group and zero-fills everything outside the level, which is exactly
-// "not water" / p = 0.  Without tensor maps the same box is loaded with
-// plain loads.
+// The box has a fixed shape per kernel (RbBox: W = 2 QW + 2 columns by
+// RH = ROWS + 2 rows), and the tile is what the halo leaves inside it:
+// TW = W - 2H by TH = RH - 2H.  Cells are stored by colour -- colour c of row
+// j is plane c, row j, index q = i >> 1, the two colours alternating along a
+// row -- so the cells one half-sweep updates and the other-colour neighbours
+// they read are contiguous, and a warp's shared-memory accesses are
+// conflict-free.  A neighbour code per cell (0: no update; else 1 + the
+// number of water neighbours) replaces the four flag tests: a non-water
+// cell's p is +0.0 and stays so, and adding +0.0 to the running neighbour
+// sum (which starts at +0.0 and never becomes -0.0 in round-to-nearest)
+// leaves it unchanged, so the sum of all four neighbours is the sum of the
+// water ones, bit for bit.  Cells outside the level load as not water, p = 0.
 //
 // Coarse levels (at most MG_SMEM_CELLS cells on the top one): one CTA runs
 // the whole remaining V-cycle in shared memory.
@@ -156,13 +164,131 @@ __global__ void k_jacobi(const __grid_constant__ Dev d, const float* __restrict_
 // the last post kernel writes pressure_a (mg_finish).  A coarse level's p
 // starts every cycle at 0 (mg_restrict zeroes it), so the pre kernels of
 // levels >= 1 do not load it.
-constexpr int BOXX = 16;  // the box starts 16 cells left of the tile (16-element aligned for TMA)
 constexpr int MG_SMEM_CELLS = 4096;
 constexpr int COARSE_THREADS = 1024;
 
-struct BoxMaps {
-  CUtensorMap p, rhs, fl;
+template <int QW_, int ROWS_>
+struct RbBox {
+  static constexpr int QW = QW_, ROWS = ROWS_;
+  static constexpr int W = 2 * QW + 2, RH = ROWS + 2;  // box columns and rows
+  static constexpr int QS = QW + 1;                    // cells of one colour in a box row
+  static constexpr int PL = RH * QS;                   // cells of one colour in the box
+  static constexpr int RPW = 32 / QW;                  // box rows a warp sweeps at once
+  static constexpr int STEPS = ROWS / (RPW * BY);      // sweep steps of a warp per half-sweep
+  static_assert(QW == 16 || QW == 32, "a box row is swept by a warp or a half-warp");
+  static_assert(ROWS % (RPW * BY) == 0, "box rows split evenly over the warps");
+  // p and rhs (float, both colours), neighbour codes (both colours), water
+  // flags (natural order, used to build the codes)
+  static constexpr size_t SMEM = (size_t)2 * PL * 4 * 2 + (size_t)2 * PL + (size_t)RH * W;
+  __host__ __device__ static constexpr int tile_w(int H) { return W - 2 * H; }
+  __host__ __device__ static constexpr int tile_h(int H) { return RH - 2 * H; }
+  __host__ __device__ static constexpr bool fits(int H) { return tile_w(H) >= 2 && tile_h(H) >= 2; }
 };
+using BoxBig = RbBox<32, 48>;    // 66 x 50 box: a 52 x 36 tile with 3 + 3 sweeps
+using BoxSmall = RbBox<16, 32>;  // 34 x 34 box: a 20 x 20 tile with 3 + 3 sweeps
+
+template <class B>
+struct RbSmem {
+  float* P;    // [2][RH][QS]
+  float* R;    // [2][RH][QS]
+  uint8_t* K;  // [2][RH][QS]
+  uint8_t* F;  // [RH][W]
+  int par;     // colour of box cell (0, 0)
+  __device__ __forceinline__ RbSmem(unsigned char* raw, int par_)
+      : P(reinterpret_cast<float*>(raw)),
+        R(P + 2 * B::PL),
+        K(reinterpret_cast<uint8_t*>(R + 2 * B::PL)),
+        F(K + 2 * B::PL),
+        par(par_) {}
+  __device__ __forceinline__ int at(int j, int i) const { return ((i + j + par) & 1) * B::PL + j * B::QS + (i >> 1); }
+};
+
+// Sum of the four neighbours of box cell (j, i) (split index a), in the order
+// of multigrid.wgsl:34-45: left, right, below, above.
+template <class B>
+__device__ __forceinline__ float rb_nb_sum(const RbSmem<B>& S, int j, int i, int a) {
+  const int o = i & 1;
+  const int b = a + (((i + j + S.par) & 1) ? -B::PL : B::PL);  // same (row, q) in the other colour
+  float s = 0.0f;
+  s += S.P[b - 1 + o];
+  s += S.P[b + o];
+  s += S.P[b - B::QS];
+  s += S.P[b + B::QS];
+  return s;
+}
+
+// Fills the box from the level: `cell(in, gi, gx, gy, f, r, p)` gives the
+// water flag, rhs and initial p of a cell (gi = its index, 0 outside the
+// level); then builds the neighbour codes.  Loads are issued for every cell
+// (index 0 outside the level) so they overlap.
+template <class B, class Fn>
+__device__ __forceinline__ void rb_load(const RbSmem<B>& S, int X0, int Y0, int nx, int ny, Fn&& cell) {
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  for (int e = tid; e < B::W * B::RH; e += BX * BY) {
+    const int j = e / B::W, i = e - j * B::W;
+    const int gx = X0 + i, gy = Y0 + j;
+    const bool in = gx >= 0 && gy >= 0 && gx < nx && gy < ny;
+    const size_t gi = in ? (size_t)gy * nx + gx : 0;
+    uint8_t f;
+    float r, p;
+    cell(in, gi, gx, gy, f, r, p);
+    const int a = S.at(j, i);
+    S.F[e] = f;
+    S.P[a] = f ? p : 0.0f;
+    S.R[a] = f ? r : 0.0f;
+  }
+  __syncthreads();
+  for (int e = tid; e < B::W * B::RH; e += BX * BY) {
+    const int j = e / B::W, i = e - j * B::W;
+    uint8_t k = 0;
+    if (i > 0 && j > 0 && i < B::W - 1 && j < B::RH - 1 && S.F[e])
+      k = (uint8_t)(1 + S.F[e - 1] + S.F[e + 1] + S.F[e - B::W] + S.F[e + B::W]);
+    S.K[S.at(j, i)] = k;
+  }
+  __syncthreads();
+}
+
+// nsweeps half-sweeps over the cells at distance >= 1 from the box edge;
+// half-sweep s updates colour (s & 1) ^ c0 (red first for c0 = 0), with the
+// update of multigrid.wgsl:60-77.
+template <class B>
+__device__ __forceinline__ void rb_sweeps(int nsweeps, int c0, float eps, const RbSmem<B>& S) {
+  const int sub = B::RPW == 1 ? 0 : (int)threadIdx.x / B::QW, ql = (int)threadIdx.x % B::QW;
+  for (int s = 0; s < nsweeps; s++) {
+    const int c = (s & 1) ^ c0;
+    float* Pc = S.P + c * B::PL;
+    const float* Po = S.P + (c ^ 1) * B::PL;
+    const float* Rc = S.R + c * B::PL;
+    const uint8_t* Kc = S.K + c * B::PL;
+#pragma unroll
+    for (int it = 0; it < B::STEPS; it++) {
+      const int j = 1 + (it * BY + (int)threadIdx.y) * B::RPW + sub;
+      const int o = (c + S.par + j) & 1;  // column parity of colour c in row j
+      const int a = j * B::QS + ql + 1 - o;  // column 2q + o, in [1, W - 2]
+      const uint8_t kk = Kc[a];
+      if (kk) {
+        float sum = 0.0f;
+        sum += Po[a - 1 + o];
+        sum += Po[a + o];
+        sum += Po[a - B::QS];
+        sum += Po[a + B::QS];
+        Pc[a] = (sum - Rc[a]) / ((float)(kk - 1) + eps);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Residual r - (s - (k + eps) p) of water cell (j, i) (multigrid.wgsl:82-105).
+template <class B>
+__device__ __forceinline__ bool rb_residual(const RbSmem<B>& S, int j, int i, float eps, float& res) {
+  const int a = S.at(j, i);
+  const uint8_t kk = S.K[a];
+  if (!kk) return false;
+  const float s = rb_nb_sum<B>(S, j, i, a);
+  res = S.R[a] - (s - ((float)(kk - 1) + eps) * S.P[a]);
+  return true;
+}
 
 // One fine level of one world in a fused pre- or post-smooth launch.
 struct MgPass {
@@ -171,14 +297,11 @@ struct MgPass {
   const float* r_src;    // right-hand side of the level
   const uint8_t* f_src;  // water flags of the level
   float* p_out;          // smoothed p of the level
-  uint32_t* status;      // the world's kernel status word
 };
-// A launch over one world's level (tensor maps in parameter space when the
-// kernel loads with TMA), or over the same level index of a batch of worlds
-// (plain loads; the CTA finds its world as the per-cell passes do).
+// A launch over one world's level, or over the same level index of a batch
+// of worlds (the CTA finds its world as the per-cell passes do).
 struct MgOne {
   MgPass e;
-  BoxMaps maps;
 };
 struct MgSet {
   const MgPass* e;
@@ -186,169 +309,68 @@ struct MgSet {
   const int* nbx;    // [n]
   int n;
 };
-__device__ __forceinline__ const BoxMaps* mg_locate(const MgOne& s, MgPass& e, int& tx, int& ty) {
+__device__ __forceinline__ void mg_locate(const MgOne& s, MgPass& e, int& tx, int& ty) {
   e = s.e;
   tx = (int)blockIdx.x;
   ty = (int)blockIdx.y;
-  return &s.maps;
 }
-__device__ __forceinline__ const BoxMaps* mg_locate(const MgSet& s, MgPass& e, int& tx, int& ty) {
+__device__ __forceinline__ void mg_locate(const MgSet& s, MgPass& e, int& tx, int& ty) {
   const int w = batch_member(s.start, s.n);
   e = s.e[w];
   const int r = (int)blockIdx.x - __ldg(s.start + w), nb = __ldg(s.nbx + w);
   tx = r % nb;
   ty = r / nb;
-  return nullptr;
-}
-template <class S>
-struct MgHasMaps {
-  static constexpr bool value = false;
-};
-template <>
-struct MgHasMaps<MgOne> {
-  static constexpr bool value = true;
-};
-
-// The neighbour sum of multigrid.wgsl:34-45 in branch-free form: adding the
-// +0.0 of a non-water neighbour leaves the running sum unchanged (it starts
-// at +0.0 and can never become -0.0 in round-to-nearest).
-__device__ __forceinline__ float gs_update(const float* sp, const float* sr, const uint8_t* sf, int c, int stride, float eps) {
-  const float fl = sf[c - 1] ? 1.0f : 0.0f, fr = sf[c + 1] ? 1.0f : 0.0f;
-  const float fb = sf[c - stride] ? 1.0f : 0.0f, ft = sf[c + stride] ? 1.0f : 0.0f;
-  float sum = 0.0f;
-  sum += fl != 0.0f ? sp[c - 1] : 0.0f;
-  sum += fr != 0.0f ? sp[c + 1] : 0.0f;
-  sum += fb != 0.0f ? sp[c - stride] : 0.0f;
-  sum += ft != 0.0f ? sp[c + stride] : 0.0f;
-  float k = 0.0f;
-  k += fl;
-  k += fr;
-  k += fb;
-  k += ft;
-  return (sum - sr[c]) / (k + eps);
 }
 
-template <int TW, int TH, bool TMA, bool TOP, bool LOADP>
-__device__ __forceinline__ bool box_load(uint32_t* status, const Lv& L, const float* __restrict__ p_src,
-                                         const float* __restrict__ r_src, const uint8_t* __restrict__ f_src,
-                                         const BoxMaps* maps, int bx, int by, int RH, float* sp, float* sr, uint8_t* sf,
-                                         uint64_t* bar) {
-  constexpr int BOXW = TW + 2 * BOXX;
-  const int n = BOXW * RH;
-  const int tid = threadIdx.y * BX + threadIdx.x;
-  if (TMA) {
-    if (tid == 0) {
-      mbar_init(bar, 1);
-      mbar_expect_tx(bar, (uint32_t)((LOADP ? 4 : 0) * n + 4 * n + n));
-      if (LOADP) tma_load_2d(sp, &maps->p, bx, by, bar);
-      tma_load_2d(sr, &maps->rhs, bx, by, bar);
-      tma_load_2d(sf, &maps->fl, bx, by, bar);
-    }
-    if (!LOADP)
-      for (int e = tid; e < n; e += BX * BY) sp[e] = 0.0f;
-    __syncthreads();
-    if (!mbar_wait_bounded(bar, 0, status)) return false;
-  } else {
-    for (int e = tid; e < n; e += BX * BY) {
-      int gx = bx + e % BOXW, gy = by + e / BOXW;
-      float p = 0.0f, r = 0.0f;
-      uint8_t f = 0;
-      if (gx >= 0 && gy >= 0 && gx < L.nx && gy < L.ny) {
-        size_t gi = (size_t)gy * L.nx + gx;
-        f = f_src[gi];
-        r = r_src[gi];
-        if (LOADP) p = p_src[gi];
-      }
-      sp[e] = p;
-      sr[e] = r;
-      sf[e] = f;
-    }
-    __syncthreads();
-  }
-  if (TOP && LOADP) {  // mg_init: p = water ? pressure_a : 0
-    for (int e = tid; e < n; e += BX * BY)
-      if (!sf[e]) sp[e] = 0.0f;
-    __syncthreads();
-  }
-  return true;
-}
-
-// Half-sweeps 0..nsweeps-1 on the box; sweep s updates the cells at distance
-// >= s+1 from the edge of the valid region (multigrid.wgsl:60-77).  Colour
-// (x + y) & 1 of sweep s is (s & 1) ^ c0: red first for c0 = 0.
-template <int TW, int TH>
-__device__ __forceinline__ void box_sweeps(int nsweeps, int H, int RH, int bx, int by, float eps, float* sp, const float* sr,
-                                           const uint8_t* sf, int c0 = 0) {
-  constexpr int BOXW = TW + 2 * BOXX;
-  const int ilo = BOXX - H, ihi = BOXX + TW + H;
-  for (int s = 0; s < nsweeps; s++) {
-    const int color = (s & 1) ^ c0;
-    const int m = s + 1;
-    for (int j = m + threadIdx.y; j < RH - m; j += BY) {
-      const int gy = by + j;
-      const int i0 = ilo + m + (((bx + ilo + m + gy) ^ color) & 1);
-      for (int i = i0 + 2 * threadIdx.x; i < ihi - m; i += 2 * BX) {
-        const int c = j * BOXW + i;
-        if (sf[c]) sp[c] = gs_update(sp, sr, sf, c, BOXW, eps);
-      }
-    }
-    __syncthreads();
-  }
-}
-
-template <int TW, int TH>
-__device__ __forceinline__ void box_store(const Lv& L, float* __restrict__ p_out, int x0, int y0, int H, const float* sp) {
-  constexpr int BOXW = TW + 2 * BOXX;
-  for (int j = threadIdx.y; j < TH; j += BY)
-    for (int i = threadIdx.x; i < TW; i += BX) {
-      int gx = x0 + i, gy = y0 + j;
-      if (gx < L.nx && gy < L.ny) p_out[(size_t)gy * L.nx + gx] = sp[(j + H) * BOXW + i + BOXX];
+// Stores the tile (box cells H.., H..) of p to a level array.
+template <class B, class St>
+__device__ __forceinline__ void rb_store_tile(const RbSmem<B>& S, int H, int x0, int y0, int nx, int ny, St&& put) {
+  const int TW = B::tile_w(H), TH = B::tile_h(H);
+  for (int y = threadIdx.y; y < TH; y += BY)
+    for (int x = threadIdx.x; x < TW; x += BX) {
+      const int gx = x0 + x, gy = y0 + y;
+      if (gx < nx && gy < ny) put((size_t)gy * nx + gx, S.P[S.at(H + y, H + x)]);
     }
 }
 
 // Pre-smooth (nu sweeps) + residual + restrict (multigrid.wgsl:60-105).
-template <int TW, int TH, bool TMA, bool TOP, class S>
+template <class B, bool TOP, class S>
 __global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ S s, int nu) {
-  static_assert(!TMA || MgHasMaps<S>::value, "TMA loads need the tensor maps of a one-world launch");
   MgPass e;
   int tile_x, tile_y;
-  const BoxMaps* maps = mg_locate(s, e, tile_x, tile_y);
+  mg_locate(s, e, tile_x, tile_y);
   const Lv& L = e.L;
   const Lv& C = e.C;
-  float* __restrict__ p_out = e.p_out;
-  constexpr int BOXW = TW + 2 * BOXX;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar;
-  const int H = 2 * nu + 1, RH = TH + 2 * H;
-  float* sp = reinterpret_cast<float*>(smem_raw);
-  float* sr = sp + BOXW * RH;
-  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int H = 2 * nu + 1, TW = B::tile_w(H), TH = B::tile_h(H);
   const int x0 = tile_x * TW, y0 = tile_y * TH;
-  const int bx = x0 - BOXX, by = y0 - H;
-  if (!box_load<TW, TH, TMA, TOP, TOP>(e.status, L, e.p_src, e.r_src, e.f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
-  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, L.eps, sp, sr, sf);
-  box_store<TW, TH>(L, p_out, x0, y0, H, sp);
+  const RbSmem<B> Sm(smem_raw, (x0 + y0) & 1);  // box cell (0, 0) is (x0 - H, y0 - H)
+  const float* __restrict__ p_src = e.p_src;
+  const float* __restrict__ r_src = e.r_src;
+  const uint8_t* __restrict__ f_src = e.f_src;
+  rb_load<B>(Sm, x0 - H, y0 - H, L.nx, L.ny, [&](bool in, size_t gi, int, int, uint8_t& f, float& r, float& p) {
+    f = in ? f_src[gi] : 0;
+    r = r_src[gi];
+    p = TOP ? p_src[gi] : 0.0f;  // mg_init: p = water ? pressure_a : 0 (levels >= 1 start at 0)
+  });
+  rb_sweeps<B>(2 * nu, 0, L.eps, Sm);
+  float* __restrict__ p_out = e.p_out;
+  rb_store_tile<B>(Sm, H, x0, y0, L.nx, L.ny, [&](size_t i, float v) { p_out[i] = v; });
   // residual of the 4 children of each coarse cell of the tile, x2 average
   for (int cj = threadIdx.y; cj < TH / 2; cj += BY)
     for (int ci = threadIdx.x; ci < TW / 2; ci += BX) {
-      int cgx = tile_x * (TW / 2) + ci, cgy = tile_y * (TH / 2) + cj;
+      const int cgx = tile_x * (TW / 2) + ci, cgy = tile_y * (TH / 2) + cj;
       if (cgx >= C.nx || cgy >= C.ny) continue;
       float sum = 0.0f;
       uint32_t nf = 0;
 #pragma unroll
       for (uint32_t q = 0; q < 4; q++) {
-        int li = BOXX + 2 * ci + (int)(q & 1u), lj = H + 2 * cj + (int)(q >> 1);
-        int c = lj * BOXW + li;
-        if (!sf[c]) continue;
-        float s = 0.0f, k = 0.0f;
-        if (sf[c - 1]) { s += sp[c - 1]; k += 1.0f; }
-        if (sf[c + 1]) { s += sp[c + 1]; k += 1.0f; }
-        if (sf[c - BOXW]) { s += sp[c - BOXW]; k += 1.0f; }
-        if (sf[c + BOXW]) { s += sp[c + BOXW]; k += 1.0f; }
-        sum += sr[c] - (s - (k + L.eps) * sp[c]);
+        float res;
+        if (!rb_residual<B>(Sm, H + 2 * cj + (int)(q >> 1), H + 2 * ci + (int)(q & 1u), L.eps, res)) continue;
+        sum += res;
         nf++;
       }
-      size_t ci_g = (size_t)cgy * C.nx + cgx;
+      const size_t ci_g = (size_t)cgy * C.nx + cgx;
       C.fl[ci_g] = nf > 0u ? 1 : 0;
       C.rhs[ci_g] = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
     }
@@ -356,34 +378,30 @@ __global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ S s, 
 
 // Prolong (add the coarse correction to water cells) + post-smooth nu sweeps
 // (multigrid.wgsl:108-114, 60-77).
-template <int TW, int TH, bool TMA, class S>
+template <class B, class S>
 __global__ void __launch_bounds__(BX* BY) k_mg_post(const __grid_constant__ S s, int nu) {
-  static_assert(!TMA || MgHasMaps<S>::value, "TMA loads need the tensor maps of a one-world launch");
   MgPass e;
   int tile_x, tile_y;
-  const BoxMaps* maps = mg_locate(s, e, tile_x, tile_y);
+  mg_locate(s, e, tile_x, tile_y);
   const Lv& L = e.L;
   const Lv& C = e.C;
-  float* __restrict__ p_out = e.p_out;
-  constexpr int BOXW = TW + 2 * BOXX;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar;
-  const int H = 2 * nu, RH = TH + 2 * H;
-  float* sp = reinterpret_cast<float*>(smem_raw);
-  float* sr = sp + BOXW * RH;
-  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int H = 2 * nu, TW = B::tile_w(H), TH = B::tile_h(H);
   const int x0 = tile_x * TW, y0 = tile_y * TH;
-  const int bx = x0 - BOXX, by = y0 - H;
-  if (!box_load<TW, TH, TMA, false, true>(e.status, L, e.p_src, e.r_src, e.f_src, maps, bx, by, RH, sp, sr, sf, &bar)) return;
-  const int n = BOXW * RH;
-  for (int e = threadIdx.y * BX + threadIdx.x; e < n; e += BX * BY) {
-    if (!sf[e]) continue;
-    int gx = bx + e % BOXW, gy = by + e / BOXW;
-    sp[e] += C.p[(size_t)(gy / 2) * C.nx + gx / 2];
-  }
-  __syncthreads();
-  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, L.eps, sp, sr, sf);
-  box_store<TW, TH>(L, p_out, x0, y0, H, sp);
+  const RbSmem<B> Sm(smem_raw, (x0 + y0) & 1);
+  const float* __restrict__ p_src = e.p_src;
+  const float* __restrict__ r_src = e.r_src;
+  const uint8_t* __restrict__ f_src = e.f_src;
+  const float* __restrict__ cp = C.p;
+  const int cnx = C.nx;
+  rb_load<B>(Sm, x0 - H, y0 - H, L.nx, L.ny, [&](bool in, size_t gi, int gx, int gy, uint8_t& f, float& r, float& p) {
+    f = in ? f_src[gi] : 0;
+    r = r_src[gi];
+    p = p_src[gi] + cp[in ? (size_t)(gy / 2) * cnx + gx / 2 : 0];
+  });
+  rb_sweeps<B>(2 * nu, 0, L.eps, Sm);
+  float* __restrict__ p_out = e.p_out;
+  rb_store_tile<B>(Sm, H, x0, y0, L.nx, L.ny, [&](size_t i, float v) { p_out[i] = v; });
 }
 
 // The V-cycle below (and including) level `top`, in one CTA.
@@ -612,17 +630,26 @@ static const char* const POST_NAMES[8] = {"mg_prolong_post_L0", "mg_prolong_post
                                           "mg_prolong_post_L3", "mg_prolong_post_L4", "mg_prolong_post_L5",
                                           "mg_prolong_post_L6", "mg_prolong_post_L7+"};
 
-// Tile shape of a fine level: 64x32 tiles where there are enough of them to
-// fill the GPU, 32x16 tiles on the smaller levels, whose kernels are bound by
+// Box of a fine level: the 66 x 50 box where its tiles are enough to fill
+// the GPU, the 34 x 34 box on the smaller levels, whose kernels are bound by
 // the latency of one tile rather than by bandwidth.
-static bool small_tiles(const MgLevel& L) {
-  const long big = (long)((L.nx + 63) / 64) * ((L.ny + 31) / 32);
+static bool small_tiles(const MgLevel& L, const MgConfig& c) {
+  const int H = 2 * c.pre + 1, tw = BoxBig::tile_w(H), th = BoxBig::tile_h(H);
+  const long big = (long)((L.nx + tw - 1) / tw) * ((L.ny + th - 1) / th);
   return big < 8 * 152;
 }
 
-template <int TW, int TH>
-static size_t box_smem(int halo) {
-  return (size_t)(TW + 2 * BOXX) * (TH + 2 * halo) * 9;
+// Tiles of a fine level's pre (halo 2 pre + 1) or post (halo 2 post) pass.
+struct TileGrid {
+  int nbx, nby;
+};
+template <class B>
+static TileGrid tile_grid(const MgLevel& L, int H) {
+  const int tw = B::tile_w(H), th = B::tile_h(H);
+  return TileGrid{(L.nx + tw - 1) / tw, (L.ny + th - 1) / th};
+}
+static TileGrid tile_grid(const MgLevel& L, bool small, int H) {
+  return small ? tile_grid<BoxSmall>(L, H) : tile_grid<BoxBig>(L, H);
 }
 
 int multigrid_first_coarse_level(const MgLevel* levels, int nl) {
@@ -632,48 +659,8 @@ int multigrid_first_coarse_level(const MgLevel* levels, int nl) {
 }
 
 bool multigrid_fused_ok(const MgLevel* levels, int nl, const MgConfig& c) {
-  if (c.pre < 1 || c.post < 1 || 2 * c.pre + 1 > BOXX || 2 * c.post > BOXX || nl > 16) return false;
+  if (c.pre < 1 || c.post < 1 || !BoxSmall::fits(2 * c.pre + 1) || !BoxSmall::fits(2 * c.post) || nl > 16) return false;
   return multigrid_first_coarse_level(levels, nl) < nl;
-}
-
-bool multigrid_make_maps(const MgLevel* levels, int nl, const MgConfig& c, const MgBufs& b, const Dev& d,
-                         MgLevelMaps* out) {
-  const int k = multigrid_first_coarse_level(levels, nl);
-  bool all = true;
-  for (int l = 0; l < k; l++) {
-    MgLevelMaps& m = out[l];
-    const bool sm = small_tiles(levels[l]);
-    const uint32_t tw = sm ? 32 : 64, th = sm ? 16 : 32, bw = tw + 2 * BOXX;
-    const uint32_t rh_pre = th + 2 * (2 * c.pre + 1), rh_post = th + 2 * (2 * c.post);
-    const uint64_t nx = levels[l].nx, ny = levels[l].ny;
-    float* rhs = l == 0 ? d.div : b.rhs + levels[l].off;
-    uint8_t* fl = b.fluid + levels[l].off;
-    float* p_pre = l == 0 ? d.pa : b.p + levels[l].off;  // only level 0 loads p before pre-smoothing
-    float* p_post = l == 0 ? b.p_tmp : b.p2 + levels[l].off;
-    bool ok = true;
-    ok &= make_tensor_map_2d(&m.pre_p, p_pre, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_pre);
-    ok &= make_tensor_map_2d(&m.pre_rhs, rhs, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_pre);
-    ok &= make_tensor_map_2d(&m.pre_fl, fl, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, nx, ny, nx, bw, rh_pre);
-    ok &= make_tensor_map_2d(&m.post_p, p_post, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_post);
-    ok &= make_tensor_map_2d(&m.post_rhs, rhs, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, nx, bw, rh_post);
-    ok &= make_tensor_map_2d(&m.post_fl, fl, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, nx, ny, nx, bw, rh_post);
-    m.ok = ok ? 1 : 0;
-    all = all && ok;
-  }
-  return all;
-}
-
-template <int TW, int TH>
-static void set_tile_attrs(int mx) {
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, true, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, true, false, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, true, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, false, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, true, MgSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_pre<TW, TH, false, false, MgSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_post<TW, TH, true, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_post<TW, TH, false, MgOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mg_post<TW, TH, false, MgSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
 static void set_smem_attrs() {
@@ -682,8 +669,6 @@ static void set_smem_attrs() {
   cudaGetDevice(&dev);
   if (attr_done >> (dev & 63) & 1ull) return;
   const int mx = 200 * 1024;
-  set_tile_attrs<64, 32>(mx);
-  set_tile_attrs<32, 16>(mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseMany>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseOne, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -695,13 +680,11 @@ static void set_smem_attrs() {
 // pressure_a; the pre-smoothed p goes to p_tmp (level 0) or p2.
 static MgPass pre_pass(const Dev& d, const MgLevel* levels, int l, const MgBufs& b) {
   const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
-  return MgPass{L, C, l == 0 ? d.pa : nullptr, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? b.p_tmp : b.p2 + levels[l].off,
-                d.status};
+  return MgPass{L, C, l == 0 ? d.pa : nullptr, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? b.p_tmp : b.p2 + levels[l].off};
 }
 static MgPass post_pass(const Dev& d, const MgLevel* levels, int l, const MgBufs& b) {
   const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
-  return MgPass{L, C, l == 0 ? b.p_tmp : b.p2 + levels[l].off, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? d.pa : L.p,
-                d.status};
+  return MgPass{L, C, l == 0 ? b.p_tmp : b.p2 + levels[l].off, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? d.pa : L.p};
 }
 static double pre_bytes(const MgLevel* levels, int l) {
   return (l == 0 ? 13.0 : 9.0) * (double)levels[l].nx * levels[l].ny + 5.0 * (double)levels[l + 1].nx * levels[l + 1].ny;
@@ -738,40 +721,25 @@ static CoarsePass coarse_pass(const Dev& d, const MgLevel* levels, int nl, const
   return e;
 }
 
-template <int TW, int TH>
+template <class B>
 static void launch_pre(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
-  MgOne one{pre_pass(d, levels, l, b), BoxMaps{}};
-  const Lv& L = one.e.L;
-  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
-  const size_t sm = box_smem<TW, TH>(2 * c.pre + 1);
-  const bool tma = b.maps && b.maps[l].ok;
-  if (tma) one.maps = BoxMaps{b.maps[l].pre_p, b.maps[l].pre_rhs, b.maps[l].pre_fl};
+  const MgOne one{pre_pass(d, levels, l, b)};
+  const TileGrid t = tile_grid<B>(levels[l], 2 * c.pre + 1);
+  const dim3 grid(t.nbx, t.nby), blk(BX, BY);
   const char* name = PRE_NAMES[l < 7 ? l : 7];
   const double bytes = pre_bytes(levels, l);
-  if (tma && l == 0)
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, true, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
-  else if (tma)
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, true, false, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
-  else if (l == 0)
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, true, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
-  else
-    RB_LAUNCH(name, bytes, s, k_mg_pre<TW, TH, false, false, MgOne><<<grid, blk, sm, s>>>(one, c.pre));
+  if (l == 0) RB_LAUNCH(name, bytes, s, k_mg_pre<B, true, MgOne><<<grid, blk, B::SMEM, s>>>(one, c.pre));
+  else RB_LAUNCH(name, bytes, s, k_mg_pre<B, false, MgOne><<<grid, blk, B::SMEM, s>>>(one, c.pre));
 }
 
-template <int TW, int TH>
+template <class B>
 static void launch_post(const Dev& d, const MgLevel* levels, int l, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
-  MgOne one{post_pass(d, levels, l, b), BoxMaps{}};
-  const Lv& L = one.e.L;
-  const dim3 grid((L.nx + TW - 1) / TW, (L.ny + TH - 1) / TH), blk(BX, BY);
-  const size_t sm = box_smem<TW, TH>(2 * c.post);
-  const bool tma = b.maps && b.maps[l].ok;
-  if (tma) one.maps = BoxMaps{b.maps[l].post_p, b.maps[l].post_rhs, b.maps[l].post_fl};
+  const MgOne one{post_pass(d, levels, l, b)};
+  const TileGrid t = tile_grid<B>(levels[l], 2 * c.post);
+  const dim3 grid(t.nbx, t.nby), blk(BX, BY);
   const double bytes = post_bytes(levels, l);
   const char* name = POST_NAMES[l < 7 ? l : 7];
-  if (tma)
-    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, true, MgOne><<<grid, blk, sm, s>>>(one, c.post));
-  else
-    RB_LAUNCH(name, bytes, s, k_mg_post<TW, TH, false, MgOne><<<grid, blk, sm, s>>>(one, c.post));
+  RB_LAUNCH(name, bytes, s, k_mg_post<B, MgOne><<<grid, blk, B::SMEM, s>>>(one, c.post));
 }
 
 void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
@@ -783,14 +751,14 @@ void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const M
   const int cycles = c.cycles < 1 ? 1 : c.cycles;
   for (int cy = 0; cy < cycles; cy++) {
     for (int l = 0; l < k; l++) {
-      if (small_tiles(levels[l])) launch_pre<32, 16>(d, levels, l, b, c, s);
-      else launch_pre<64, 32>(d, levels, l, b, c, s);
+      if (small_tiles(levels[l], c)) launch_pre<BoxSmall>(d, levels, l, b, c, s);
+      else launch_pre<BoxBig>(d, levels, l, b, c, s);
     }
     RB_LAUNCH("mg_coarse_vcycle", coarse_bytes, s,
               k_mg_coarse<CoarseOne><<<1, COARSE_THREADS, coarse_smem, s>>>(co, c.pre, c.post, c.coarse));
     for (int l = k - 1; l >= 0; l--) {
-      if (small_tiles(levels[l])) launch_post<32, 16>(d, levels, l, b, c, s);
-      else launch_post<64, 32>(d, levels, l, b, c, s);
+      if (small_tiles(levels[l], c)) launch_post<BoxSmall>(d, levels, l, b, c, s);
+      else launch_post<BoxBig>(d, levels, l, b, c, s);
     }
   }
 }
@@ -804,14 +772,19 @@ void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const M
 // as when it is stepped alone.
 
 struct MgBatchPlan {
+  // One fine level index and box shape over the worlds that have it; the
+  // pre and post passes tile the level differently (their halos differ).
   struct Group {
     int level;   // fine level index
-    bool small;  // 32x16 tiles (else 64x32)
-    int n, total;
+    bool small;  // BoxSmall (else BoxBig)
+    int n;
     const MgPass* pre;  // device [n]
     const MgPass* post;
-    const int* start;  // device [n + 1]
-    const int* nbx;    // device [n]
+    int total_pre, total_post;
+    const int* start_pre;  // device [n + 1]: first CTA of each world
+    const int* start_post;
+    const int* nbx_pre;    // device [n]: tiles per row of each world
+    const int* nbx_post;
     double bytes_pre, bytes_post;
   };
   MgConfig c{};
@@ -837,7 +810,7 @@ MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, c
     return off;
   };
   struct Offs {
-    size_t pre, post, start, nbx;
+    size_t pre, post, start_pre, start_post, nbx_pre, nbx_post;
   };
   std::vector<Offs> offs;
   for (int w = 0; w < n; w++) {
@@ -847,20 +820,21 @@ MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, c
   for (int l = 0; l < plan->levels; l++) {
     for (int small = 0; small < 2; small++) {
       std::vector<MgPass> pre, post;
-      std::vector<int> start(1, 0), nbx;
+      std::vector<int> start_pre(1, 0), start_post(1, 0), nbx_pre, nbx_post;
       double bpre = 0.0, bpost = 0.0;
       for (int w = 0; w < n; w++) {
         const MgWorld& W = ws[w];
         if (l >= multigrid_first_coarse_level(W.levels, W.nlevels)) continue;
         const int mode = l < nmodes ? tile_mode[l] : 0;
-        const bool sm = mode == 1 ? false : (mode == 2 ? true : small_tiles(W.levels[l]));
+        const bool sm = mode == 1 ? false : (mode == 2 ? true : small_tiles(W.levels[l], c));
         if (sm != (small != 0)) continue;
-        const int tw = sm ? 32 : 64, th = sm ? 16 : 32;
-        const int bx = (W.levels[l].nx + tw - 1) / tw, by = (W.levels[l].ny + th - 1) / th;
+        const TileGrid tp = tile_grid(W.levels[l], sm, 2 * c.pre + 1), tq = tile_grid(W.levels[l], sm, 2 * c.post);
         pre.push_back(pre_pass(W.d, W.levels, l, W.b));
         post.push_back(post_pass(W.d, W.levels, l, W.b));
-        nbx.push_back(bx);
-        start.push_back(start.back() + bx * by);
+        nbx_pre.push_back(tp.nbx);
+        nbx_post.push_back(tq.nbx);
+        start_pre.push_back(start_pre.back() + tp.nbx * tp.nby);
+        start_post.push_back(start_post.back() + tq.nbx * tq.nby);
         bpre += pre_bytes(W.levels, l);
         bpost += post_bytes(W.levels, l);
       }
@@ -869,12 +843,16 @@ MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, c
       g.level = l;
       g.small = small != 0;
       g.n = (int)pre.size();
-      g.total = start.back();
+      g.total_pre = start_pre.back();
+      g.total_post = start_post.back();
       g.bytes_pre = bpre;
       g.bytes_post = bpost;
       plan->groups.push_back(g);
       offs.push_back(Offs{put(pre.data(), pre.size() * sizeof(MgPass)), put(post.data(), post.size() * sizeof(MgPass)),
-                          put(start.data(), start.size() * sizeof(int)), put(nbx.data(), nbx.size() * sizeof(int))});
+                          put(start_pre.data(), start_pre.size() * sizeof(int)),
+                          put(start_post.data(), start_post.size() * sizeof(int)),
+                          put(nbx_pre.data(), nbx_pre.size() * sizeof(int)),
+                          put(nbx_post.data(), nbx_post.size() * sizeof(int))});
     }
   }
   std::vector<CoarsePass> co;
@@ -900,10 +878,13 @@ MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, c
   }
   unsigned char* base = static_cast<unsigned char*>(plan->blob);
   for (size_t i = 0; i < plan->groups.size(); i++) {
-    plan->groups[i].pre = reinterpret_cast<const MgPass*>(base + offs[i].pre);
-    plan->groups[i].post = reinterpret_cast<const MgPass*>(base + offs[i].post);
-    plan->groups[i].start = reinterpret_cast<const int*>(base + offs[i].start);
-    plan->groups[i].nbx = reinterpret_cast<const int*>(base + offs[i].nbx);
+    MgBatchPlan::Group& g = plan->groups[i];
+    g.pre = reinterpret_cast<const MgPass*>(base + offs[i].pre);
+    g.post = reinterpret_cast<const MgPass*>(base + offs[i].post);
+    g.start_pre = reinterpret_cast<const int*>(base + offs[i].start_pre);
+    g.start_post = reinterpret_cast<const int*>(base + offs[i].start_post);
+    g.nbx_pre = reinterpret_cast<const int*>(base + offs[i].nbx_pre);
+    g.nbx_post = reinterpret_cast<const int*>(base + offs[i].nbx_post);
   }
   plan->coarse = reinterpret_cast<const CoarsePass*>(base + co_off);
   return plan;
@@ -917,35 +898,29 @@ void multigrid_batch_free(MgBatchPlan* plan) {
 
 int multigrid_batch_levels(const MgBatchPlan* plan) { return plan ? plan->levels : 0; }
 
-static void launch_group_pre(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
-  const MgSet set{g.pre, g.start, g.nbx, g.n};
-  const dim3 blk(BX, BY);
+template <class B>
+static void launch_group_pre_b(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
+  const MgSet set{g.pre, g.start_pre, g.nbx_pre, g.n};
   const char* name = PRE_NAMES[g.level < 7 ? g.level : 7];
-  if (g.small) {
-    const size_t sm = box_smem<32, 16>(2 * c.pre + 1);
-    if (g.level == 0)
-      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<32, 16, false, true, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
-    else
-      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<32, 16, false, false, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
-  } else {
-    const size_t sm = box_smem<64, 32>(2 * c.pre + 1);
-    if (g.level == 0)
-      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<64, 32, false, true, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
-    else
-      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<64, 32, false, false, MgSet><<<g.total, blk, sm, s>>>(set, c.pre));
-  }
+  if (g.level == 0)
+    RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, true, MgSet><<<g.total_pre, dim3(BX, BY), B::SMEM, s>>>(set, c.pre));
+  else
+    RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, false, MgSet><<<g.total_pre, dim3(BX, BY), B::SMEM, s>>>(set, c.pre));
+}
+static void launch_group_pre(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
+  if (g.small) launch_group_pre_b<BoxSmall>(g, c, s);
+  else launch_group_pre_b<BoxBig>(g, c, s);
 }
 
-static void launch_group_post(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
-  const MgSet set{g.post, g.start, g.nbx, g.n};
-  const dim3 blk(BX, BY);
+template <class B>
+static void launch_group_post_b(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
+  const MgSet set{g.post, g.start_post, g.nbx_post, g.n};
   const char* name = POST_NAMES[g.level < 7 ? g.level : 7];
-  if (g.small)
-    RB_LAUNCH(name, g.bytes_post, s,
-              k_mg_post<32, 16, false, MgSet><<<g.total, blk, box_smem<32, 16>(2 * c.post), s>>>(set, c.post));
-  else
-    RB_LAUNCH(name, g.bytes_post, s,
-              k_mg_post<64, 32, false, MgSet><<<g.total, blk, box_smem<64, 32>(2 * c.post), s>>>(set, c.post));
+  RB_LAUNCH(name, g.bytes_post, s, k_mg_post<B, MgSet><<<g.total_post, dim3(BX, BY), B::SMEM, s>>>(set, c.post));
+}
+static void launch_group_post(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
+  if (g.small) launch_group_post_b<BoxSmall>(g, c, s);
+  else launch_group_post_b<BoxBig>(g, c, s);
 }
 
 void launch_multigrid_batch(const MgBatchPlan* plan, cudaStream_t s) {
@@ -1015,63 +990,34 @@ __device__ __forceinline__ float mp_ld(const __half* p, size_t i) { return __hal
 __device__ __forceinline__ void mp_st(float* p, size_t i, float v) { p[i] = v; }
 __device__ __forceinline__ void mp_st(__half* p, size_t i, float v) { p[i] = __float2half_rn(v); }
 
-// Loads the box of a level: the right-hand side (level 0: the CG residual
-// minus its component's mean, times the FP16 scale), the water flags and,
-// for post-smoothing, e_f plus alpha times the coarse total correction.
-template <int TW, int TH, bool TOP, class T>
-__device__ __forceinline__ void mp_load(const MpLevelArgs& a, int bx, int by, int H, int RH, bool post, float* sp,
-                                        float* sr, uint8_t* sf) {
-  // Only the columns the sweeps and the restriction touch (H cells either
-  // side of the tile); the alignment margin of the TMA box stays unused.
-  // Every load is issued unconditionally (clamped index) so they overlap.
-  constexpr int BOXW = TW + 2 * BOXX;
-  const int W = TW + 2 * H, i0 = BOXX - H;
-  const int n = W * RH, tid = threadIdx.y * BX + threadIdx.x;
-  const float sc = TOP ? a.scale[0] : 1.0f;
-  for (int e = tid; e < n; e += BX * BY) {
-    const int i = i0 + e % W, j = e / W;
-    const int gx = bx + i, gy = by + j;
-    const bool in = gx >= 0 && gy >= 0 && gx < a.nx && gy < a.ny;
-    const size_t gi = in ? (size_t)gy * a.nx + gx : 0;
-    const uint8_t f = in ? a.fl[gi] : 0;
-    float r, p = 0.0f;
-    if (TOP) {
-      const float rr = static_cast<const float*>(a.rhs)[gi];
-      const int lab = a.label[gi];
-      r = (rr - a.comp_mean[lab < 0 ? 0 : lab]) * sc;
-    } else {
-      r = mp_ld(static_cast<const T*>(a.rhs), gi);
-    }
-    if (post) {
-      const size_t ci = in ? (size_t)(gy / 2) * a.cnx + gx / 2 : 0;
-      p = mp_ld(static_cast<const T*>(a.ef), gi) + a.alpha * a.cE[ci];
-    }
-    const int c = j * BOXW + i;
-    sp[c] = f ? p : 0.0f;
-    sr[c] = f ? r : 0.0f;
-    sf[c] = f;
+// The right-hand side of a level's cell: level 0 the CG residual minus its
+// component's mean, times the FP16 scale; below, the stored restriction.
+template <bool TOP, class T>
+__device__ __forceinline__ float mp_rhs(const MpLevelArgs& a, size_t gi, float sc) {
+  if (TOP) {
+    const float rr = static_cast<const float*>(a.rhs)[gi];
+    const int lab = a.label[gi];
+    return (rr - a.comp_mean[lab < 0 ? 0 : lab]) * sc;
   }
-  __syncthreads();
+  return mp_ld(static_cast<const T*>(a.rhs), gi);
 }
 
 // Pre-smooth from zero + residual + restriction (1/2 * sum over water children).
-template <int TW, int TH, bool TOP, class T, class CT>
+template <class B, bool TOP, class T, class CT>
 __global__ void __launch_bounds__(BX* BY) k_mp_pre(const __grid_constant__ MpLevelArgs a, int nu) {
-  constexpr int BOXW = TW + 2 * BOXX;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  const int H = 2 * nu + 1, RH = TH + 2 * H;
-  float* sp = reinterpret_cast<float*>(smem_raw);
-  float* sr = sp + BOXW * RH;
-  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
-  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, bx = x0 - BOXX, by = y0 - H;
-  mp_load<TW, TH, TOP, T>(a, bx, by, H, RH, false, sp, sr, sf);
-  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, a.eps, sp, sr, sf, 0);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int H = 2 * nu + 1, TW = B::tile_w(H), TH = B::tile_h(H);
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+  const RbSmem<B> Sm(smem_raw, (x0 + y0) & 1);
+  const float sc = TOP ? a.scale[0] : 1.0f;
+  rb_load<B>(Sm, x0 - H, y0 - H, a.nx, a.ny, [&](bool in, size_t gi, int, int, uint8_t& f, float& r, float& p) {
+    f = in ? a.fl[gi] : 0;
+    r = mp_rhs<TOP, T>(a, gi, sc);
+    p = 0.0f;
+  });
+  rb_sweeps<B>(2 * nu, 0, a.eps, Sm);
   T* ef = static_cast<T*>(a.ef);
-  for (int j = threadIdx.y; j < TH; j += BY)
-    for (int i = threadIdx.x; i < TW; i += BX) {
-      const int gx = x0 + i, gy = y0 + j;
-      if (gx < a.nx && gy < a.ny) mp_st(ef, (size_t)gy * a.nx + gx, sp[(j + H) * BOXW + i + BOXX]);
-    }
+  rb_store_tile<B>(Sm, H, x0, y0, a.nx, a.ny, [&](size_t i, float v) { mp_st(ef, i, v); });
   CT* crhs = static_cast<CT*>(a.crhs);
   for (int cj = threadIdx.y; cj < TH / 2; cj += BY)
     for (int ci = threadIdx.x; ci < TW / 2; ci += BX) {
@@ -1081,14 +1027,9 @@ __global__ void __launch_bounds__(BX* BY) k_mp_pre(const __grid_constant__ MpLev
       uint32_t nf = 0;
 #pragma unroll
       for (uint32_t q = 0; q < 4; q++) {
-        const int c = (H + 2 * cj + (int)(q >> 1)) * BOXW + BOXX + 2 * ci + (int)(q & 1u);
-        if (!sf[c]) continue;
-        float s = 0.0f, k = 0.0f;
-        if (sf[c - 1]) { s += sp[c - 1]; k += 1.0f; }
-        if (sf[c + 1]) { s += sp[c + 1]; k += 1.0f; }
-        if (sf[c - BOXW]) { s += sp[c - BOXW]; k += 1.0f; }
-        if (sf[c + BOXW]) { s += sp[c + BOXW]; k += 1.0f; }
-        sum += sr[c] - (s - (k + a.eps) * sp[c]);
+        float res;
+        if (!rb_residual<B>(Sm, H + 2 * cj + (int)(q >> 1), H + 2 * ci + (int)(q & 1u), a.eps, res)) continue;
+        sum += res;
         nf++;
       }
       mp_st(crhs, (size_t)cgy * a.cnx + cgx, nf > 0u ? 0.5f * sum : 0.0f);
@@ -1096,25 +1037,25 @@ __global__ void __launch_bounds__(BX* BY) k_mp_pre(const __grid_constant__ MpLev
 }
 
 // Prolong (alpha * coarse total) + post-smooth (colours reversed).
-template <int TW, int TH, bool TOP, class T>
+template <class B, bool TOP, class T>
 __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLevelArgs a, int nu) {
-  constexpr int BOXW = TW + 2 * BOXX;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double zsh[BX * BY / 32];
   __shared__ int dom;
-  const int H = 2 * nu, RH = TH + 2 * H;
-  float* sp = reinterpret_cast<float*>(smem_raw);
-  float* sr = sp + BOXW * RH;
-  uint8_t* sf = reinterpret_cast<uint8_t*>(sr + BOXW * RH);
-  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, bx = x0 - BOXX, by = y0 - H;
-  mp_load<TW, TH, TOP, T>(a, bx, by, H, RH, true, sp, sr, sf);
-  box_sweeps<TW, TH>(2 * nu, H, RH, bx, by, a.eps, sp, sr, sf, 1);
+  const int H = 2 * nu, TW = B::tile_w(H), TH = B::tile_h(H);
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+  const RbSmem<B> Sm(smem_raw, (x0 + y0) & 1);
+  const float sc = TOP ? a.scale[0] : 1.0f;
+  rb_load<B>(Sm, x0 - H, y0 - H, a.nx, a.ny, [&](bool in, size_t gi, int gx, int gy, uint8_t& f, float& r, float& p) {
+    f = in ? a.fl[gi] : 0;
+    r = mp_rhs<TOP, T>(a, gi, sc);
+    const size_t ci = in ? (size_t)(gy / 2) * a.cnx + gx / 2 : 0;
+    p = mp_ld(static_cast<const T*>(a.ef), gi) + a.alpha * a.cE[ci];
+  });
+  rb_sweeps<B>(2 * nu, 1, a.eps, Sm);
   if (!TOP) {
-    for (int j = threadIdx.y; j < TH; j += BY)
-      for (int i = threadIdx.x; i < TW; i += BX) {
-        const int gx = x0 + i, gy = y0 + j;
-        if (gx < a.nx && gy < a.ny) a.E[(size_t)gy * a.nx + gx] = sp[(j + H) * BOXW + i + BOXX];
-      }
+    float* E = a.E;
+    rb_store_tile<B>(Sm, H, x0, y0, a.nx, a.ny, [&](size_t i, float v) { E[i] = v; });
     return;
   }
   if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -1135,7 +1076,7 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
       if (gx >= a.nx || gy >= a.ny) continue;
       const size_t gi = (size_t)gy * a.nx + gx;
       const int lab = a.label[gi];
-      const float z = lab >= 0 ? sp[(j + H) * BOXW + i + BOXX] * inv : 0.0f;
+      const float z = lab >= 0 ? Sm.P[Sm.at(H + j, H + i)] * inv : 0.0f;
       a.z[gi] = z;
       if (lab >= 0) {
         if (lab == dom) own += z;
@@ -1157,20 +1098,6 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
   }
 }
 
-template <int TW, int TH>
-void mp_attrs(int mx) {
-  cudaFuncSetAttribute(k_mp_pre<TW, TH, true, __half, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_pre<TW, TH, true, __half, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_pre<TW, TH, false, __half, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_pre<TW, TH, false, __half, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_pre<TW, TH, false, float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_pre<TW, TH, true, float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_post<TW, TH, true, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_post<TW, TH, true, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_post<TW, TH, false, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_mp_post<TW, TH, false, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-}
-
 const char* const MP_PRE_NAMES[8] = {"mp_pre_L0", "mp_pre_L1", "mp_pre_L2", "mp_pre_L3",
                                      "mp_pre_L4", "mp_pre_L5", "mp_pre_L6", "mp_pre_L7+"};
 const char* const MP_POST_NAMES[8] = {"mp_post_L0", "mp_post_L1", "mp_post_L2", "mp_post_L3",
@@ -1181,53 +1108,51 @@ const char* const MP_POST_NAMES[8] = {"mp_post_L0", "mp_post_L1", "mp_post_L2", 
 // correction is written (2 or 4), the coarse rhs written (a quarter size);
 // post reads e_f, rhs, flag and a quarter-size coarse total and writes the
 // total (z and its label read on level 0).
-template <int TW, int TH>
-void mp_launch_pre(const MpLevelArgs& a, int l, bool top, bool half, bool chalf, int nu, cudaStream_t s) {
-  const dim3 grid((a.nx + TW - 1) / TW, (a.ny + TH - 1) / TH), blk(BX, BY);
-  const size_t sm = box_smem<TW, TH>(2 * nu + 1);
+template <class B>
+void mp_launch_pre(const MpLevelArgs& a, const MgLevel& L, int l, bool top, bool half, bool chalf, int nu, cudaStream_t s) {
+  const TileGrid t = tile_grid<B>(L, 2 * nu + 1);
+  const dim3 grid(t.nbx, t.nby), blk(BX, BY);
+  const size_t sm = B::SMEM;
   const double es = half ? 2.0 : 4.0, n = (double)a.nx * a.ny;
   const double bytes = n * ((top ? 9.0 : es + 1.0) + es + (chalf ? 2.0 : 4.0) / 4.0);
   const char* name = MP_PRE_NAMES[l < 7 ? l : 7];
-  if (top && half && chalf) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, true, __half, __half><<<grid, blk, sm, s>>>(a, nu));
-  else if (top && half) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, true, __half, float><<<grid, blk, sm, s>>>(a, nu));
-  else if (top) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, true, float, float><<<grid, blk, sm, s>>>(a, nu));
-  else if (half && chalf) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, false, __half, __half><<<grid, blk, sm, s>>>(a, nu));
-  else if (half) RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, false, __half, float><<<grid, blk, sm, s>>>(a, nu));
-  else RB_LAUNCH(name, bytes, s, k_mp_pre<TW, TH, false, float, float><<<grid, blk, sm, s>>>(a, nu));
+  if (top && half && chalf) RB_LAUNCH(name, bytes, s, k_mp_pre<B, true, __half, __half><<<grid, blk, sm, s>>>(a, nu));
+  else if (top && half) RB_LAUNCH(name, bytes, s, k_mp_pre<B, true, __half, float><<<grid, blk, sm, s>>>(a, nu));
+  else if (top) RB_LAUNCH(name, bytes, s, k_mp_pre<B, true, float, float><<<grid, blk, sm, s>>>(a, nu));
+  else if (half && chalf) RB_LAUNCH(name, bytes, s, k_mp_pre<B, false, __half, __half><<<grid, blk, sm, s>>>(a, nu));
+  else if (half) RB_LAUNCH(name, bytes, s, k_mp_pre<B, false, __half, float><<<grid, blk, sm, s>>>(a, nu));
+  else RB_LAUNCH(name, bytes, s, k_mp_pre<B, false, float, float><<<grid, blk, sm, s>>>(a, nu));
 }
 
-template <int TW, int TH>
-void mp_launch_post(const MpLevelArgs& a, int l, bool top, bool half, int nu, cudaStream_t s) {
-  const dim3 grid((a.nx + TW - 1) / TW, (a.ny + TH - 1) / TH), blk(BX, BY);
-  const size_t sm = box_smem<TW, TH>(2 * nu);
+template <class B>
+void mp_launch_post(const MpLevelArgs& a, const MgLevel& L, int l, bool top, bool half, int nu, cudaStream_t s) {
+  const TileGrid t = tile_grid<B>(L, 2 * nu);
+  const dim3 grid(t.nbx, t.nby), blk(BX, BY);
+  const size_t sm = B::SMEM;
   const double es = half ? 2.0 : 4.0, n = (double)a.nx * a.ny;
   const double bytes = n * (es + (top ? 9.0 : es + 1.0) + 1.0 + (top ? 8.0 : 4.0));
   const char* name = MP_POST_NAMES[l < 7 ? l : 7];
-  if (top && half) RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, true, __half><<<grid, blk, sm, s>>>(a, nu));
-  else if (top) RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, true, float><<<grid, blk, sm, s>>>(a, nu));
-  else if (half) RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, false, __half><<<grid, blk, sm, s>>>(a, nu));
-  else RB_LAUNCH(name, bytes, s, k_mp_post<TW, TH, false, float><<<grid, blk, sm, s>>>(a, nu));
+  if (top && half) RB_LAUNCH(name, bytes, s, k_mp_post<B, true, __half><<<grid, blk, sm, s>>>(a, nu));
+  else if (top) RB_LAUNCH(name, bytes, s, k_mp_post<B, true, float><<<grid, blk, sm, s>>>(a, nu));
+  else if (half) RB_LAUNCH(name, bytes, s, k_mp_post<B, false, __half><<<grid, blk, sm, s>>>(a, nu));
+  else RB_LAUNCH(name, bytes, s, k_mp_post<B, false, float><<<grid, blk, sm, s>>>(a, nu));
 }
 
 }  // namespace
 
-void multigrid_prepare_mixed() {
-  static uint64_t attr_done = 0;  // one bit per device
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (!(attr_done >> (dev & 63) & 1ull)) {
-    mp_attrs<64, 32>(200 * 1024);
-    mp_attrs<32, 16>(200 * 1024);
-    attr_done |= 1ull << (dev & 63);
-  }
-  set_smem_attrs();
+void multigrid_prepare_mixed() { set_smem_attrs(); }
+
+size_t mixed_vcycle_tiles(const MgLevel* levels, int nl, const MgConfig& c) {
+  (void)nl;
+  const TileGrid t = tile_grid(levels[0], small_tiles(levels[0], c), 2 * c.post);
+  return (size_t)t.nbx * t.nby;
 }
 
 int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MpHierarchy& h,
                         cudaStream_t s) {
   multigrid_prepare_mixed();
   const int k = multigrid_first_coarse_level(levels, nl);
-  int launches = 0;
+  const MgConfig c{h.pre, h.post, 0, 1};
   auto args = [&](int l) {
     MpLevelArgs a{};
     a.nx = levels[l].nx;
@@ -1251,15 +1176,11 @@ int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBuf
     a.part_dom = h.part_dom;
     return a;
   };
-  const bool small0 = small_tiles(levels[0]);
-  const int tw0 = small0 ? 32 : 64, th0 = small0 ? 16 : 32;
-  const int tiles0 = ((levels[0].nx + tw0 - 1) / tw0) * ((levels[0].ny + th0 - 1) / th0);
   for (int l = 0; l < k; l++) {
     const MpLevelArgs a = args(l);
     const bool half = l < h.nhalf, chalf = l + 1 < k && l + 1 < h.nhalf;
-    if (small_tiles(levels[l])) mp_launch_pre<32, 16>(a, l, l == 0, half, chalf, h.pre, s);
-    else mp_launch_pre<64, 32>(a, l, l == 0, half, chalf, h.pre, s);
-    launches++;
+    if (small_tiles(levels[l], c)) mp_launch_pre<BoxSmall>(a, levels[l], l, l == 0, half, chalf, h.pre, s);
+    else mp_launch_pre<BoxBig>(a, levels[l], l, l == 0, half, chalf, h.pre, s);
   }
   size_t coarse_smem = 0;
   double coarse_bytes = 0.0;
@@ -1268,16 +1189,13 @@ int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBuf
   co.e.alpha = h.alpha;
   RB_LAUNCH("mp_coarse_vcycle", coarse_bytes, s,
             k_mg_coarse<CoarseOne, true><<<1, COARSE_THREADS, coarse_smem, s>>>(co, h.pre, h.post, 0));
-  launches++;
   for (int l = k - 1; l >= 0; l--) {
     const MpLevelArgs a = args(l);
     const bool half = l < h.nhalf;
-    if (small_tiles(levels[l])) mp_launch_post<32, 16>(a, l, l == 0, half, h.post, s);
-    else mp_launch_post<64, 32>(a, l, l == 0, half, h.post, s);
-    launches++;
+    if (small_tiles(levels[l], c)) mp_launch_post<BoxSmall>(a, levels[l], l, l == 0, half, h.post, s);
+    else mp_launch_post<BoxBig>(a, levels[l], l, l == 0, half, h.post, s);
   }
-  (void)launches;
-  return tiles0;
+  return (int)mixed_vcycle_tiles(levels, nl, c);
 }
 
 }  // namespace ribo

@@ -139,11 +139,6 @@ extern "C" ribo_status ribo_pressure_solve_noalloc(uint32_t fluid_w, uint32_t fl
   d.fluid0 = b.fluid + levels[0].off;
   d.status = status;
 
-  MgLevelMaps maps[16];
-  memset(maps, 0, sizeof maps);
-  multigrid_make_maps(levels, nl, c, b, d, maps);  // levels that cannot use TMA load with plain loads
-  b.maps = maps;
-
   // The status word must start at zero; everything else is written before
   // it is read within the call.
   st = cuda_status(cudaMemsetAsync(status, 0, 4, stream), "status");

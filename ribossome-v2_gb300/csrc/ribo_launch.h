@@ -94,20 +94,12 @@ struct MgLevel {
   size_t off;  // element offset of the level in the level arrays
   float eps;
 };
-// TMA tensor maps of one fine level of the fused V-cycle: the boxes the
-// pre-smooth kernel loads (p only on level 0, rhs, water flags) and the
-// boxes the post-smooth kernel loads (pre-smoothed p, rhs, water flags).
-struct MgLevelMaps {
-  CUtensorMap pre_p, pre_rhs, pre_fl, post_p, post_rhs, post_fl;
-  int ok;
-};
 struct MgBufs {
   float* p;         // all levels, contiguous (64-element aligned level offsets)
   float* rhs;       // all levels
   uint8_t* fluid;   // all levels: 1 = water
   float* p_tmp;     // level-0 ping-pong partner of pressure_a (fused path)
   float* p2;        // all levels: pre-smoothed p (fused path)
-  const MgLevelMaps* maps;  // host array, one per level, or null (plain loads)
 };
 struct MgConfig {
   int pre, post, coarse, cycles;
@@ -116,13 +108,9 @@ struct MgConfig {
 void launch_multigrid(const Dev& d, const MgLevel* levels, int nlevels, const MgBufs& b, const MgConfig& c, cudaStream_t s);
 // The same V-cycles, bit-identical: fused tile kernels per fine level and one
 // shared-memory kernel for the coarse levels.  Usable when the coarsest level
-// fits in shared memory and 1 <= pre, post <= 8.
+// fits in shared memory and 1 <= pre <= 7, 1 <= post <= 8.
 bool multigrid_fused_ok(const MgLevel* levels, int nlevels, const MgConfig& c);
 int multigrid_first_coarse_level(const MgLevel* levels, int nlevels);
-// Encodes the tensor maps of the fine levels; false when some level cannot
-// use TMA (its kernels then load with plain loads).
-bool multigrid_make_maps(const MgLevel* levels, int nlevels, const MgConfig& c, const MgBufs& b, const Dev& d,
-                         MgLevelMaps* out);
 void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nlevels, const MgBufs& b, const MgConfig& c,
                             cudaStream_t s);
 void launch_jacobi(const Dev& d, int iters, cudaStream_t s);
@@ -174,6 +162,9 @@ struct MpHierarchy {
 };
 // Sets the kernel attributes of the mixed V-cycle (call before capturing it).
 void multigrid_prepare_mixed();
+// Level-0 tiles of the mixed V-cycle's post pass (entries of part_c /
+// part_dom it writes).
+size_t mixed_vcycle_tiles(const MgLevel* levels, int nlevels, const MgConfig& c);
 // Launches one V-cycle of the preconditioner; returns the number of level-0
 // tiles (entries of part_c / part_dom it wrote).
 int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nlevels, const MgBufs& b, const MpHierarchy& h,

@@ -101,7 +101,6 @@ struct World {
   MixedSolver* mixed = nullptr;      // precision_mode = RIBO_PRECISION_MIXED
   ribo_status solve_error = RIBO_OK;  // a pressure solve that failed to record
   MgBufs mg{};
-  std::vector<MgLevelMaps> mg_maps;
   uint32_t* status = nullptr;  // kernel error bits (RIBO_ERR_*)
   // per-step parameters: two slots of 64 copies, device + pinned staging
   ribo_sim_params* d_params = nullptr;

@@ -219,7 +219,7 @@ static void keep_pool_memory(int dev) {
 
 // Multigrid levels (src/world/mod.rs:637-671): halve while both sides are
 // above the minimum and even; eps = MG_EPS * 2^l.  Returns the elements of
-// the level arrays (64-element aligned level bases: TMA wants 16-byte bases).
+// the level arrays (64-element aligned level bases).
 static size_t build_levels(int fw, int fh, uint32_t min_size, std::vector<MgLevel>& levels) {
   levels.clear();
   int nx = fw, ny = fh, l = 0;
@@ -333,13 +333,6 @@ ribo_status World::init(const ribo_world_cfg& c) {
   }
   // gamma = 0 at creation: derive slope and mask once.
   Dev d = dev();
-  {
-    MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, 1};
-    mg_maps.assign(levels.size(), MgLevelMaps{});
-    if (multigrid_fused_ok(levels.data(), (int)levels.size(), c))
-      multigrid_make_maps(levels.data(), (int)levels.size(), c, mg, d, mg_maps.data());
-    mg.maps = mg_maps.data();
-  }
   launch_slope(d, (float)cfg.world_units_per_cell, stream);
   launch_solid_mask(target_one(d, nullptr), stream);
   RB_TRY(cudaGetLastError(), "init kernels");

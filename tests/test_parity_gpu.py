@@ -23,8 +23,8 @@ CASES = [
     ("long-displacement-rubble", 160, 80, dict(BASE, dt=9.0, cohesion=0.7, monomer_pressure=1.0, aggregation=0.1),
      dict(fluid_substep=1), 4, dict(rubble_frac=0.2, max_disp=2.5, dt=9.0)),
     ("crowded-cells", 96, None, dict(BASE, settle=2.0), dict(fluid_substep=1), 4, dict(monomer_mean=40.0, rubble_frac=0.1)),
-    # 200 is not a multiple of 16: the fused V-cycle stages its tiles with plain loads instead of TMA
-    ("200-plain-load-tiles", 200, None, BASE, dict(fluid_substep=1, mg_cycles=2), 3, dict(mg_pre=3, mg_post=3)),
+    # 200 is not a multiple of the tile sizes: partial tiles at the right and top edges
+    ("200-partial-tiles", 200, None, BASE, dict(fluid_substep=1, mg_cycles=2), 3, dict(mg_pre=3, mg_post=3)),
     ("test-cfg-256-128-defaults", 256, 128, dict(dt=1.0), {}, 8, {}),
     ("64-reference-constants", 64, None, dict(BASE, diffusion=30.0, settle=1.0, thermal_activation=1.0,
                                               aggregation=0.02), dict(fluid_substep=1), 10, {}),
