@@ -363,7 +363,9 @@ def run_ours(args):
                 "share_of_step": tms / max(sum(v[1] for v in kern.values()), 1e-9)}
     step_rl = {"bytes_per_step": step_bytes, "achieved": step_bytes / (ms / args.steps * 1e-3) / 1e9,
                "frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}
-    breakdown = sorted(((k, v[1] / prof_steps, v[0] // prof_steps) for k, v in kern.items()), key=lambda x: -x[1])
+    # [pass, ms per step, launches per step, algorithmic GB/s], every pass
+    breakdown = sorted(((k, v[1] / prof_steps, v[0] // prof_steps, v[2] / max(v[1], 1e-9) / 1e6) for k, v in kern.items()),
+                       key=lambda x: -x[1])
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -371,7 +373,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
         "config": dict(workload_config(n), parallelism=f"replicas x{ws}" if ws > 1 else "single world"),
         "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "step_roofline": step_rl,
-        "kernels_ms_per_step": [[k, round(t, 4), c] for k, t, c in breakdown[:12]],
+        "kernels_ms_per_step": [[k, round(t, 4), c, round(g, 1)] for k, t, c, g in breakdown],
         "clocks": clk,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -409,30 +409,32 @@ __global__ void __launch_bounds__(NF_THREADS) k_net_flux(const __grid_constant__
   // of the chunk; of a column block: position u of line `lane`
   auto load = [&](int c, int b, int lw) {
     const int k0 = c * NF_C;
-    float v[NF_UPW];
-    bool wet[NF_UPW];
+    float2 sv[NF_UPW];
+    uint8_t wall[NF_UPW];
+    bool in[NF_UPW];
 #pragma unroll
-    for (int q = 0; q < NF_UPW; q++) {
+    for (int q = 0; q < NF_UPW; q++) {  // loads only, all in flight together
       const int u = lw + NF_LOADERS * q;
       const int l = rows ? u / (NF_C / 32) : lane, k = rows ? (u % (NF_C / 32)) * 32 + lane : u;
       const int line = line0 + l, pos = k0 + k;
-      const bool in = u < NF_C && line < nlines && pos < len;
-      const size_t i = in ? (rows ? (size_t)line * d.fw + pos : (size_t)pos * d.fw + line) : 0;
-      const float2 sv = sanitize(vin[i]);
-      wet[q] = in && !mask[i];
-      v[q] = rows ? sv.y : sv.x;
+      in[q] = u < NF_C && line < nlines && pos < len;
+      const size_t i = in[q] ? (rows ? (size_t)line * d.fw + pos : (size_t)pos * d.fw + line) : 0;
+      sv[q] = __ldg(vin + i);
+      wall[q] = __ldg(mask + i);
     }
 #pragma unroll
     for (int q = 0; q < NF_UPW; q++) {
       const int u = lw + NF_LOADERS * q;
       if (u >= NF_C) continue;  // uniform over the warp
       const int l = rows ? u / (NF_C / 32) : lane, k = rows ? (u % (NF_C / 32)) * 32 + lane : u;
-      val[b][l][k] = wet[q] ? v[q] : 0.0f;
+      const bool wet_q = in[q] && !wall[q];
+      const float2 s2 = sanitize(sv[q]);
+      val[b][l][k] = wet_q ? (rows ? s2.y : s2.x) : 0.0f;
       if (rows) {
-        const uint32_t m = __ballot_sync(0xffffffffu, wet[q]);
+        const uint32_t m = __ballot_sync(0xffffffffu, wet_q);
         if (lane == 0 && m) atomicAdd(&wet_cells[l], (uint32_t)__popc(m));
       } else {
-        my_wet += wet[q] ? 1u : 0u;
+        my_wet += wet_q ? 1u : 0u;
       }
     }
   };

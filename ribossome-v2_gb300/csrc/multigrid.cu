@@ -224,18 +224,30 @@ __device__ __forceinline__ float rb_nb_sum(const RbSmem<B>& S, int j, int i, int
 template <class B, class Fn>
 __device__ __forceinline__ void rb_load(const RbSmem<B>& S, int X0, int Y0, int nx, int ny, Fn&& cell) {
   const int tid = threadIdx.y * BX + threadIdx.x;
-  for (int e = tid; e < B::W * B::RH; e += BX * BY) {
-    const int j = e / B::W, i = e - j * B::W;
-    const int gx = X0 + i, gy = Y0 + j;
-    const bool in = gx >= 0 && gy >= 0 && gx < nx && gy < ny;
-    const size_t gi = in ? (size_t)gy * nx + gx : 0;
-    uint8_t f;
-    float r, p;
-    cell(in, gi, gx, gy, f, r, p);
-    const int a = S.at(j, i);
-    S.F[e] = f;
-    S.P[a] = f ? p : 0.0f;
-    S.R[a] = f ? r : 0.0f;
+  constexpr int N = B::W * B::RH, NT = BX * BY, IT = (N + NT - 1) / NT, BATCH = 4;
+#pragma unroll
+  for (int it0 = 0; it0 < IT; it0 += BATCH) {
+    uint8_t f[BATCH];
+    float r[BATCH], p[BATCH];
+#pragma unroll
+    for (int u = 0; u < BATCH; u++) {  // a batch's loads are all issued before its stores
+      const int e = tid + (it0 + u) * NT;
+      const int j = e / B::W, i = e - j * B::W;
+      const int gx = X0 + i, gy = Y0 + j;
+      const bool in = it0 + u < IT && e < N && gx >= 0 && gy >= 0 && gx < nx && gy < ny;
+      const size_t gi = in ? (size_t)gy * nx + gx : 0;
+      cell(in, gi, gx, gy, f[u], r[u], p[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < BATCH; u++) {
+      const int e = tid + (it0 + u) * NT;
+      if (it0 + u >= IT || e >= N) continue;
+      const int j = e / B::W, i = e - j * B::W;
+      const int a = S.at(j, i);
+      S.F[e] = f[u];
+      S.P[a] = f[u] ? p[u] : 0.0f;
+      S.R[a] = f[u] ? r[u] : 0.0f;
+    }
   }
   __syncthreads();
   for (int e = tid; e < B::W * B::RH; e += BX * BY) {
@@ -409,7 +421,8 @@ struct CoarseSet {
   int n;  // levels in the set (top .. coarsest)
   int nx[16], ny[16];
   float eps[16];
-  int off[16];  // cell offset of each level in shared memory
+  int off[16];  // first cell of each level's padded colour planes in shared memory
+  int total;    // cells of all levels' planes
   const float* rhs_top;
   const uint8_t* fl_top;
   float* p_out;  // level `top` result
@@ -442,24 +455,89 @@ struct CoarseMany {
 __device__ __forceinline__ const CoarsePass& coarse_of(const CoarseOne& s) { return s.e; }
 __device__ __forceinline__ const CoarsePass& coarse_of(const CoarseMany& s) { return s.e[blockIdx.x]; }
 
-// One colour of a red-black sweep on a level held in shared memory: the
-// block is viewed as 32 x (COARSE_THREADS/32) threads walking the cells of
-// that colour only.
-__device__ __forceinline__ void sm_sweep(int nx, int ny, float eps, float* p, const float* r, const uint8_t* f, uint32_t color) {
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, rows = COARSE_THREADS / 32;
-  for (int y = ty; y < ny; y += rows) {
-    for (int x = 2 * tx + (int)(((uint32_t)y + color) & 1u); x < nx; x += 64) {
-      const int idx = y * nx + x;
-      if (!f[idx]) continue;
-      float s = 0.0f, k = 0.0f;
-      if (x > 0 && f[idx - 1]) { s += p[idx - 1]; k += 1.0f; }
-      if (x + 1 < nx && f[idx + 1]) { s += p[idx + 1]; k += 1.0f; }
-      if (y > 0 && f[idx - nx]) { s += p[idx - nx]; k += 1.0f; }
-      if (y + 1 < ny && f[idx + nx]) { s += p[idx + nx]; k += 1.0f; }
-      p[idx] = (s - r[idx]) / (k + eps);
+// A coarse level in shared memory: the level plus a ring of non-water cells,
+// (nx + 2) x (ny + 2), stored by colour like the fine boxes (plane
+// (i + j) & 1, row j, index i >> 1 in padded coordinates), with the same
+// neighbour codes, so its sweeps read contiguous, conflict-free words and
+// need no flag tests or bounds checks.
+__host__ __device__ constexpr int coarse_qs(int nx) { return (nx + 3) / 2; }
+__host__ __device__ constexpr int coarse_cells(int nx, int ny) { return 2 * (ny + 2) * coarse_qs(nx); }
+struct CLv {
+  int nx, ny, qs, pl;
+  float eps;
+  float* P;
+  float* R;
+  uint8_t* K;
+  uint8_t* F;
+  __device__ __forceinline__ int at(int y, int x) const {  // level cell (x, y)
+    const int j = y + 1, i = x + 1;
+    return ((i + j) & 1) * pl + j * qs + (i >> 1);
+  }
+};
+__device__ __forceinline__ CLv coarse_level(const CoarseSet& cs, unsigned char* smem, int l) {
+  CLv L;
+  L.nx = cs.nx[l];
+  L.ny = cs.ny[l];
+  L.qs = coarse_qs(L.nx);
+  L.pl = (L.ny + 2) * L.qs;
+  L.eps = cs.eps[l];
+  float* base = reinterpret_cast<float*>(smem);
+  L.P = base + cs.off[l];
+  L.R = base + cs.total + cs.off[l];
+  L.K = reinterpret_cast<uint8_t*>(base + 2 * cs.total) + cs.off[l];
+  L.F = L.K + cs.total;
+  return L;
+}
+// Neighbour codes from the water flags (F) of a level.
+__device__ __forceinline__ void coarse_codes(const CLv& L) {
+  for (int e = threadIdx.x; e < L.nx * L.ny; e += COARSE_THREADS) {
+    const int y = e / L.nx, x = e - y * L.nx;
+    const int a = L.at(y, x);
+    uint8_t k = 0;
+    if (L.F[a]) {
+      const int o = (x + 1) & 1, b = a + (((x + y) & 1) ? -L.pl : L.pl);
+      k = (uint8_t)(1 + L.F[b - 1 + o] + L.F[b + o] + L.F[b - L.qs] + L.F[b + L.qs]);
+    }
+    L.K[a] = k;
+  }
+}
+// One colour of a red-black sweep (multigrid.wgsl:60-77): warps take rows,
+// lanes the colour's cells of the row.
+__device__ __forceinline__ void coarse_sweep(const CLv& L, int c) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* Pc = L.P + c * L.pl;
+  const float* Po = L.P + (c ^ 1) * L.pl;
+  const float* Rc = L.R + c * L.pl;
+  const uint8_t* Kc = L.K + c * L.pl;
+  for (int j = 1 + warp; j <= L.ny; j += COARSE_THREADS / 32) {
+    const int o = (c + j) & 1;  // padded column parity of colour c in row j
+    for (int q = lane + 1 - o; 2 * q + o <= L.nx; q += 32) {
+      const int a = j * L.qs + q;
+      const uint8_t kk = Kc[a];
+      if (!kk) continue;
+      float sum = 0.0f;
+      sum += Po[a - 1 + o];
+      sum += Po[a + o];
+      sum += Po[a - L.qs];
+      sum += Po[a + L.qs];
+      Pc[a] = (sum - Rc[a]) / ((float)(kk - 1) + L.eps);
     }
   }
   __syncthreads();
+}
+// Residual of level cell (x, y) if it is water (multigrid.wgsl:82-105).
+__device__ __forceinline__ bool coarse_residual(const CLv& L, int y, int x, float& res) {
+  const int a = L.at(y, x);
+  const uint8_t kk = L.K[a];
+  if (!kk) return false;
+  const int o = (x + 1) & 1, b = a + (((x + y) & 1) ? -L.pl : L.pl);
+  float s = 0.0f;
+  s += L.P[b - 1 + o];
+  s += L.P[b + o];
+  s += L.P[b - L.qs];
+  s += L.P[b + L.qs];
+  res = L.R[a] - (s - ((float)(kk - 1) + L.eps) * L.P[a]);
+  return true;
 }
 
 template <class S, bool MP = false>
@@ -467,19 +545,23 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
   const CoarsePass& e = coarse_of(s);
   const CoarseSet& cs = e.cs;
   const bool TOP = e.top != 0;
-  extern __shared__ float smem[];
-  int total = cs.off[cs.n - 1] + cs.nx[cs.n - 1] * cs.ny[cs.n - 1];
-  float* P = smem;
-  float* R = P + total;
-  uint8_t* F = reinterpret_cast<uint8_t*>(R + total);
+  extern __shared__ __align__(16) unsigned char smem[];
+  // every plane cell starts as non-water, p = rhs = 0 (the rings stay so)
   {
-    const int n = cs.nx[0] * cs.ny[0];
-    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    float* f = reinterpret_cast<float*>(smem);
+    for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) f[i] = 0.0f;
+    uint8_t* b = reinterpret_cast<uint8_t*>(f + 2 * cs.total);
+    for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) b[i] = 0;
+  }
+  __syncthreads();
+  {
+    const CLv L = coarse_level(cs, smem, 0);
+    for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
+      const int y = idx / L.nx, x = idx - y * L.nx;
       uint8_t f;
       float r, p = 0.0f;
       if (TOP) {
-        int y = idx / cs.nx[0], x = idx - y * cs.nx[0];
-        size_t gi = (size_t)y * e.fw + x;
+        const size_t gi = (size_t)y * e.fw + x;
         f = e.mask[gi] ? 0 : 1;
         r = e.div[gi];
         p = f ? e.pa[gi] : 0.0f;
@@ -487,98 +569,89 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
         f = cs.fl_top[idx];
         r = cs.rhs_top[idx];
       }
-      P[idx] = p;
-      R[idx] = r;
-      F[idx] = f;
+      const int a = L.at(y, x);
+      L.F[a] = f;
+      L.P[a] = f ? p : 0.0f;
+      L.R[a] = f ? r : 0.0f;
     }
+    __syncthreads();
+    coarse_codes(L);
+    __syncthreads();
   }
-  __syncthreads();
   for (int l = 0; l + 1 < cs.n; l++) {
-    float* p = P + cs.off[l];
-    const float* r = R + cs.off[l];
-    const uint8_t* f = F + cs.off[l];
+    const CLv L = coarse_level(cs, smem, l), C = coarse_level(cs, smem, l + 1);
     for (int k = 0; k < nu_pre; k++) {
-      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p,r, f, 0u);
-      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], p,r, f, 1u);
+      coarse_sweep(L, 0);
+      coarse_sweep(L, 1);
     }
-    const int nx = cs.nx[l], ny = cs.ny[l], cnx = cs.nx[l + 1], cny = cs.ny[l + 1];
-    float* pc = P + cs.off[l + 1];
-    float* rc = R + cs.off[l + 1];
-    uint8_t* fc = F + cs.off[l + 1];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, rows = COARSE_THREADS / 32;
-    for (int cy = ty; cy < cny; cy += rows)
-    for (int cx = tx; cx < cnx; cx += 32) {
-      const int cidx = cy * cnx + cx;
+    for (int ci = threadIdx.x; ci < C.nx * C.ny; ci += COARSE_THREADS) {
+      const int cy = ci / C.nx, cx = ci - cy * C.nx;
       float sum = 0.0f;
       uint32_t nf = 0;
       for (uint32_t q = 0; q < 4; q++) {
-        int x = cx * 2 + (int)(q & 1u), y = cy * 2 + (int)(q >> 1);
-        int i = y * nx + x;
-        if (!f[i]) continue;
-        float s = 0.0f, k = 0.0f;
-        if (x > 0 && f[i - 1]) { s += p[i - 1]; k += 1.0f; }
-        if (x + 1 < nx && f[i + 1]) { s += p[i + 1]; k += 1.0f; }
-        if (y > 0 && f[i - nx]) { s += p[i - nx]; k += 1.0f; }
-        if (y + 1 < ny && f[i + nx]) { s += p[i + nx]; k += 1.0f; }
-        sum += r[i] - (s - (k + cs.eps[l]) * p[i]);
+        float res;
+        if (!coarse_residual(L, cy * 2 + (int)(q >> 1), cx * 2 + (int)(q & 1u), res)) continue;
+        sum += res;
         nf++;
       }
-      fc[cidx] = nf > 0u ? 1 : 0;
-      if (MP) rc[cidx] = nf > 0u ? 0.5f * sum : 0.0f;
-      else rc[cidx] = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
-      pc[cidx] = 0.0f;
+      const int a = C.at(cy, cx);
+      C.F[a] = nf > 0u ? 1 : 0;
+      if (MP) C.R[a] = nf > 0u ? 0.5f * sum : 0.0f;
+      else C.R[a] = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
+      C.P[a] = 0.0f;
     }
+    __syncthreads();
+    coarse_codes(C);
     __syncthreads();
   }
-  if (MP) {
-    // exact coarsest solve in FP64: one warp per row of the dense inverse
-    const int l = cs.n - 1, nc = cs.nx[l] * cs.ny[l];
-    const float* rc = R + cs.off[l];
-    float* pcst = P + cs.off[l];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = warp; i < nc; i += COARSE_THREADS / 32) {
-      const double* row = e.inv + (size_t)i * nc;
-      double acc = 0.0;
-      for (int j = lane; j < nc; j += 32) acc += row[j] * (double)rc[j];
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-      if (lane == 0) pcst[i] = (float)acc;
-    }
-    __syncthreads();
-  } else {
-    const int l = cs.n - 1;
-    for (int k = 0; k < coarse; k++) {
-      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], P + cs.off[l], R + cs.off[l], F + cs.off[l], 0u);
-      sm_sweep(cs.nx[l], cs.ny[l], cs.eps[l], P + cs.off[l], R + cs.off[l], F + cs.off[l], 1u);
+  {
+    const CLv L = coarse_level(cs, smem, cs.n - 1);
+    if (MP) {
+      // exact coarsest solve in FP64: one warp per row of the dense inverse
+      // (the inverse indexes the level's cells in row-major order)
+      const int nc = L.nx * L.ny;
+      float* rn = reinterpret_cast<float*>(smem + (size_t)10 * cs.total);
+      for (int i = threadIdx.x; i < nc; i += COARSE_THREADS) rn[i] = L.R[L.at(i / L.nx, i % L.nx)];
+      __syncthreads();
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int i = warp; i < nc; i += COARSE_THREADS / 32) {
+        const double* row = e.inv + (size_t)i * nc;
+        double acc = 0.0;
+        for (int j = lane; j < nc; j += 32) acc += row[j] * (double)rn[j];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) L.P[L.at(i / L.nx, i % L.nx)] = (float)acc;
+      }
+      __syncthreads();
+    } else {
+      for (int k = 0; k < coarse; k++) {
+        coarse_sweep(L, 0);
+        coarse_sweep(L, 1);
+      }
     }
   }
   for (int l = cs.n - 2; l >= 0; l--) {
-    float* p = P + cs.off[l];
-    const float* pc = P + cs.off[l + 1];
-    const float* r = R + cs.off[l];
-    const uint8_t* f = F + cs.off[l];
-    const int nx = cs.nx[l], cnx = cs.nx[l + 1];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, rows = COARSE_THREADS / 32;
-    for (int y = ty; y < cs.ny[l]; y += rows)
-      for (int x = tx; x < nx; x += 32) {
-        const int idx = y * nx + x;
-        if (f[idx]) p[idx] += MP ? e.alpha * pc[(y / 2) * cnx + x / 2] : pc[(y / 2) * cnx + x / 2];
-      }
+    const CLv L = coarse_level(cs, smem, l), C = coarse_level(cs, smem, l + 1);
+    for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
+      const int y = idx / L.nx, x = idx - y * L.nx;
+      const int a = L.at(y, x);
+      if (!L.K[a]) continue;
+      const float pc = C.P[C.at(y / 2, x / 2)];
+      L.P[a] += MP ? e.alpha * pc : pc;
+    }
     __syncthreads();
-    const uint32_t c0 = MP ? 1u : 0u;
+    const int c0 = MP ? 1 : 0;
     for (int k = 0; k < nu_post; k++) {
-      sm_sweep(nx, cs.ny[l], cs.eps[l], p,r, f, c0);
-      sm_sweep(nx, cs.ny[l], cs.eps[l], p,r, f, c0 ^ 1u);
+      coarse_sweep(L, c0);
+      coarse_sweep(L, c0 ^ 1);
     }
   }
   {
-    const int n = cs.nx[0] * cs.ny[0];
-    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
-      if (TOP) {
-        int y = idx / cs.nx[0], x = idx - y * cs.nx[0];
-        e.pa[(size_t)y * e.fw + x] = P[idx];
-      } else {
-        cs.p_out[idx] = P[idx];
-      }
+    const CLv L = coarse_level(cs, smem, 0);
+    for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
+      const int y = idx / L.nx, x = idx - y * L.nx;
+      const float v = L.P[L.at(y, x)];
+      if (TOP) e.pa[(size_t)y * e.fw + x] = v;
+      else cs.p_out[idx] = v;
     }
   }
 }
@@ -658,9 +731,20 @@ int multigrid_first_coarse_level(const MgLevel* levels, int nl) {
   return k;
 }
 
+// Shared memory of the coarse kernel: the padded colour planes of every
+// coarse level (p, rhs: 4 bytes; codes, flags: 1 byte) and a row-major copy
+// of the coarsest rhs for the FP64 dense solve.
+static size_t coarse_smem_bytes(const MgLevel* levels, int nl) {
+  const int k = multigrid_first_coarse_level(levels, nl);
+  size_t cells = 0;
+  for (int l = k; l < nl; l++) cells += (size_t)coarse_cells(levels[l].nx, levels[l].ny);
+  return cells * 10 + (size_t)levels[nl - 1].nx * levels[nl - 1].ny * 4;
+}
+constexpr size_t COARSE_SMEM_MAX = 200 * 1024;
+
 bool multigrid_fused_ok(const MgLevel* levels, int nl, const MgConfig& c) {
   if (c.pre < 1 || c.post < 1 || !BoxSmall::fits(2 * c.pre + 1) || !BoxSmall::fits(2 * c.post) || nl > 16) return false;
-  return multigrid_first_coarse_level(levels, nl) < nl;
+  return multigrid_first_coarse_level(levels, nl) < nl && coarse_smem_bytes(levels, nl) <= COARSE_SMEM_MAX;
 }
 
 static void set_smem_attrs() {
@@ -668,7 +752,7 @@ static void set_smem_attrs() {
   int dev = 0;
   cudaGetDevice(&dev);
   if (attr_done >> (dev & 63) & 1ull) return;
-  const int mx = 200 * 1024;
+  const int mx = (int)COARSE_SMEM_MAX;
   cudaFuncSetAttribute(k_mg_coarse<CoarseOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseMany>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseOne, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -706,8 +790,9 @@ static CoarsePass coarse_pass(const Dev& d, const MgLevel* levels, int nl, const
     cs.ny[l - k] = levels[l].ny;
     cs.eps[l - k] = levels[l].eps;
     cs.off[l - k] = off;
-    off += levels[l].nx * levels[l].ny;
+    off += coarse_cells(levels[l].nx, levels[l].ny);
   }
+  cs.total = off;
   cs.rhs_top = b.rhs + levels[k].off;
   cs.fl_top = b.fluid + levels[k].off;
   cs.p_out = b.p + levels[k].off;
@@ -716,7 +801,7 @@ static CoarsePass coarse_pass(const Dev& d, const MgLevel* levels, int nl, const
   e.pa = d.pa;
   e.fw = d.fw;
   e.top = k == 0 ? 1 : 0;
-  *smem = (size_t)off * 9 + 16;
+  *smem = coarse_smem_bytes(levels, nl);
   *bytes = 13.0 * levels[k].nx * levels[k].ny;
   return e;
 }
@@ -1058,15 +1143,22 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
     rb_store_tile<B>(Sm, H, x0, y0, a.nx, a.ny, [&](size_t i, float v) { E[i] = v; });
     return;
   }
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    int d = -1;
-    for (int j = 0; j < TH && d < 0; j++)
-      for (int i = 0; i < TW && d < 0; i++) {
+  // the tile's dominant component: that of its first water cell in row-major order
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  if (tid == 0) dom = 0x7fffffff;
+  __syncthreads();
+  {
+    int first = 0x7fffffff;
+    for (int j = threadIdx.y; j < TH; j += BY)
+      for (int i = threadIdx.x; i < TW; i += BX) {
         const int gx = x0 + i, gy = y0 + j;
-        if (gx < a.nx && gy < a.ny) d = a.label[(size_t)gy * a.nx + gx];
+        if (gx < a.nx && gy < a.ny && a.label[(size_t)gy * a.nx + gx] >= 0) first = min(first, j * TW + i);
       }
-    dom = d;
+    for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+    if ((tid & 31) == 0 && first != 0x7fffffff) atomicMin(&dom, first);
   }
+  __syncthreads();
+  if (tid == 0) dom = dom == 0x7fffffff ? -1 : a.label[(size_t)(y0 + dom / TW) * a.nx + x0 + dom % TW];
   __syncthreads();
   const float inv = a.scale[1];
   float own = 0.0f;
@@ -1086,7 +1178,6 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
   // the tile's partial for its dominant component (FP64 above the thread level)
   double t = (double)own;
   for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-  const int tid = threadIdx.y * BX + threadIdx.x;
   if ((tid & 31) == 0) zsh[tid >> 5] = t;
   __syncthreads();
   if (tid == 0) {
