@@ -141,12 +141,14 @@ __device__ __forceinline__ float rubble_drag(const Dev& d, uint32_t x, uint32_t 
       uint32_t c = __ldg(d.gamma + (size_t)(y * d.ry + dy) * d.gw + x * d.rx + dx);
       if (c < GAMMA_SOLID) g += (float)c;
     }
+  if (g == 0.0f) return 1.0f;  // 1 / (1 + 0): no rubble under the cell
   g = g / ((float)(d.rx * d.ry) * (float)GAMMA_SOLID);
   return 1.0f / (1.0f + RUBBLE_DRAG * g * dt);
 }
 // fluid.wgsl:165-178
 __device__ __forceinline__ float2 slope_steer(const Dev& d, const ribo_sim_params* P, uint32_t x, uint32_t y, float2 v_in, float dt) {
   float2 s0 = sanitize(d.slope[env_cell_for_fluid(d, x, y)]);
+  if (s0.x == 0.0f && s0.y == 0.0f) return v_in;  // s_len = 0 < 1e-5
   float2 s = f2(-s0.x, -s0.y);
   float v_len = len2(v_in), s_len = len2(s);
   if (v_len < (float)1e-5 || s_len < (float)1e-5) return v_in;
@@ -185,7 +187,8 @@ __global__ void k_add_forces(const __grid_constant__ S s, int dir) {
   float2 f_user = clamp_len(mix2(f_c, f_avg, FORCE_SMOOTH_MIX), MAX_FORCE);
   float2 v = sanitize(add2(sanitize(vin[idx]), mul2(f_user, dt)));
   v = slope_steer(d, P, x, y, v, dt);
-  v = mul2(v, rubble_drag(d, x, y, dt));
+  const float drag = rubble_drag(d, x, y, dt);
+  if (drag != 1.0f) v = mul2(v, drag);  // v * 1 is v
   v = reflect_if_into_solid(d, x, y, v);
   vout[idx] = clamp_len(v, MAX_VEL);
 }

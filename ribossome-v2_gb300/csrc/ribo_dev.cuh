@@ -215,9 +215,14 @@ __device__ __forceinline__ float2 reflect_n(float2 n, float2 v_in) {
   return v_in;
 }
 // The wall normal depends on the mask alone, so it is computed once per
-// mask build (k_wall_normals) and read here: same function, same bits.
+// mask build (k_wall_normals) and read here: same function, same bits.  A
+// stored normal is either exactly (0, 0) or of length about 1 (solid_normal
+// divides by a length above 1e-6), so "length > 1e-6" is "not (0, 0)".
 __device__ __forceinline__ float2 reflect_if_into_solid(const Dev& d, uint32_t x, uint32_t y, float2 v) {
-  return reflect_n(d.normal[(size_t)y * d.fw + x], v);
+  const float2 n = d.normal[(size_t)y * d.fw + x];
+  if (n.x == 0.0f && n.y == 0.0f) return v;
+  const float dd = dot2(v, n);
+  return dd < 0.0f ? sub2(v, mul2(n, dd)) : v;
 }
 // fluid.wgsl:191-194 on an arbitrary input buffer
 __device__ __forceinline__ float2 raw_velocity_cell(const Dev& d, const float2* vin, uint32_t x, uint32_t y) {

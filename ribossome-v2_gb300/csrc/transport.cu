@@ -353,7 +353,8 @@ struct Smem {
   uint16_t slot[16][NT];           // accumulator slot of each window bin (blocking resolved), or FAR
   uint32_t off[TY][4 * TX + 1];    // per warp: exclusive prefix of movers over (cell, channel)
   uint32_t accum[AC][4];           // tile + ring destination sums [cell][channel]
-  uint8_t rock[AC], full[AC];
+  uint8_t rock[AC];                // destination is rock
+  uint8_t blk[AC];                 // bit 0: blocks a monomer from a non-rock cell, bit 1: from a rock cell
   float cohf[16];                  // 1 + cohesion * m for m = 0..8 (1 where cohesion is off)
   float2 lattice[4][4];            // smooth_start lattice values of this tile
   float2 jit, glob;                // smooth_start per-step jitter and offset
@@ -413,7 +414,9 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       full = cell_total4(load_cell(d.chem, t)) > capacity_of(g);
     }
     S.rock[e] = rock;
-    S.full[e] = full;
+    // rock blocks monomers from non-rock cells; a full cell blocks everyone
+    // else (transport.wgsl:364-401)
+    S.blk[e] = (uint8_t)((rock || full ? 1u : 0u) | (!rock && full ? 2u : 0u));
   }
   // smooth_start (transport.wgsl:95-117): the per-step jitter and offset and
   // the lattice values this tile can touch are computed once per CTA.
@@ -555,31 +558,40 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         S.acc[k][tid] = acc[k];
         S.acc[4 + k][tid] = accs[k];
       }
-      // destination slot of every window bin (transport.wgsl:364-401)
-#pragma unroll 4
-      for (int b = 0; b < 16; b++) {
-        int tx = iclamp((int)x + basex + (b & 3), 0, (int)G - 1);
-        int ty = iclamp((int)y + basey + (b >> 2), 0, (int)GH - 1);
-        int ax = tx - (X0 - st::HALO), ay = ty - (Y0 - st::HALO);
-        const bool near = ax >= 0 && ax < st::AW && ay >= 0 && ay < st::AH;
-        uint16_t sl;
-        if (tx == (int)x && ty == (int)y) {
-          sl = (uint16_t)(say * st::AW + sax);
-        } else {
-          bool rock, full;
-          if (near) {
-            rock = S.rock[ay * st::AW + ax];
-            full = S.full[ay * st::AW + ax];
-          } else {
-            size_t t = (size_t)ty * G + tx;
-            uint32_t g_t = __ldg(d.gamma + t);
-            rock = g_t >= GAMMA_SOLID;
-            full = cell_total4(load_cell(d.chem, t)) > capacity_of(g_t);
-          }
-          const bool blocked = rock ? (g_src < GAMMA_SOLID) : full;
-          sl = blocked ? (uint16_t)(say * st::AW + sax) : (near ? (uint16_t)(ay * st::AW + ax) : st::FAR);
+      // destination slot of every window bin (transport.wgsl:364-401); the
+      // window's columns and rows are clamped and located once
+      {
+        const uint16_t own = (uint16_t)(say * st::AW + sax);
+        const uint32_t src_bit = g_src >= GAMMA_SOLID ? 1u : 0u;
+        int txs[4], axs[4];
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+          txs[o] = iclamp((int)x + basex + o, 0, (int)G - 1);
+          axs[o] = txs[o] - (X0 - st::HALO);
         }
-        S.slot[b][tid] = sl;
+        for (int oy = 0; oy < 4; oy++) {
+          const int ty = iclamp((int)y + basey + oy, 0, (int)GH - 1), ay = ty - (Y0 - st::HALO);
+          const bool near_y = ay >= 0 && ay < st::AH;
+#pragma unroll
+          for (int ox = 0; ox < 4; ox++) {
+            const int ax = axs[ox];
+            uint16_t sl;
+            if (txs[ox] == (int)x && ty == (int)y) {
+              sl = own;
+            } else if (near_y && ax >= 0 && ax < st::AW) {
+              const int cell = ay * st::AW + ax;
+              sl = (S.blk[cell] >> src_bit) & 1u ? own : (uint16_t)cell;
+            } else {
+              const size_t t = (size_t)ty * G + txs[ox];
+              const uint32_t g_t = __ldg(d.gamma + t);
+              const bool rock = g_t >= GAMMA_SOLID;
+              const bool full = cell_total4(load_cell(d.chem, t)) > capacity_of(g_t);
+              const bool blocked = rock ? (g_src < GAMMA_SOLID) : full;
+              sl = blocked ? own : st::FAR;
+            }
+            S.slot[oy * 4 + ox][tid] = sl;
+          }
+        }
       }
       // local reactions per channel (transport.wgsl:262-294)
       const uint32_t words[4] = {cw.x, cw.y, cw.z, cw.w};
