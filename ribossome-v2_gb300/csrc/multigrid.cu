@@ -703,13 +703,14 @@ static const char* const POST_NAMES[8] = {"mg_prolong_post_L0", "mg_prolong_post
                                           "mg_prolong_post_L3", "mg_prolong_post_L4", "mg_prolong_post_L5",
                                           "mg_prolong_post_L6", "mg_prolong_post_L7+"};
 
-// Box of a fine level: the 66 x 50 box where its tiles are enough to fill
-// the GPU, the 34 x 34 box on the smaller levels, whose kernels are bound by
-// the latency of one tile rather than by bandwidth.
+// Box of a fine level: the 66 x 50 box where it gives at least three tiles
+// per SM (152 SMs), the 34 x 34 box on the smaller levels, whose kernels are
+// bound by the latency of one tile rather than by bandwidth (measured on the
+// 2048^2 levels: 1024^2 is faster with the big box, 512^2 with the small).
 static bool small_tiles(const MgLevel& L, const MgConfig& c) {
   const int H = 2 * c.pre + 1, tw = BoxBig::tile_w(H), th = BoxBig::tile_h(H);
   const long big = (long)((L.nx + tw - 1) / tw) * ((L.ny + th - 1) / th);
-  return big < 8 * 152;
+  return big < 3 * 152;
 }
 
 // Tiles of a fine level's pre (halo 2 pre + 1) or post (halo 2 post) pass.
