@@ -172,7 +172,10 @@ struct RbBox {
   static constexpr int QW = QW_, ROWS = ROWS_;
   static constexpr int W = 2 * QW + 2, RH = ROWS + 2;  // box columns and rows
   static constexpr int QS = QW + 1;                    // cells of one colour in a box row
-  static constexpr int PL = RH * QS;                   // cells of one colour in the box
+  // stride of a colour plane: its RH x QS cells, padded to 16 words past a
+  // multiple of 32 so that lanes alternating between the planes (natural
+  // order loads and stores) hit distinct banks
+  static constexpr int PL = RH * QS + ((16 - (RH * QS) % 32) + 32) % 32;
   static constexpr int RPW = 32 / QW;                  // box rows a warp sweeps at once
   static constexpr int STEPS = ROWS / (RPW * BY);      // sweep steps of a warp per half-sweep
   static_assert(QW == 16 || QW == 32, "a box row is swept by a warp or a half-warp");

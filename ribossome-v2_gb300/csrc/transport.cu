@@ -352,10 +352,12 @@ struct Smem {
   uint32_t segw[4][NT];            // per channel: activated count | neighbour counts (above)
   uint16_t slot[16][NT];           // accumulator slot of each window bin (blocking resolved), or FAR
   uint32_t off[TY][4 * TX + 1];    // per warp: exclusive prefix of movers over (cell, channel)
-  uint32_t accum[AC][4];           // tile + ring destination sums [cell][channel]
+  uint32_t accum[4][AC];           // tile + ring destination sums [channel][cell] (lanes on
+                                   // neighbouring cells hit neighbouring banks)
   uint8_t rock[AC];                // destination is rock
   uint8_t blk[AC];                 // bit 0: blocks a monomer from a non-rock cell, bit 1: from a rock cell
   float cohf[16];                  // 1 + cohesion * m for m = 0..8 (1 where cohesion is off)
+  float exp_dec[8];                // expected decays for min(act, 8) = 1..8
   float2 lattice[4][4];            // smooth_start lattice values of this tile
   float2 jit, glob;                // smooth_start per-step jitter and offset
 };
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
 
   // ---- zero the accumulator, load the blocking flags of tile + ring ----
   for (int e = tid; e < st::AC; e += st::NT) {
-    S.accum[e][0] = S.accum[e][1] = S.accum[e][2] = S.accum[e][3] = 0u;
+    S.accum[0][e] = S.accum[1][e] = S.accum[2][e] = S.accum[3][e] = 0u;
     int gx = X0 - st::HALO + e % st::AW, gy = Y0 - st::HALO + e / st::AW;
     uint8_t rock = 0, full = 0;
     if (gx >= 0 && gy >= 0 && gx < (int)G && gy < (int)GH) {
@@ -436,6 +438,13 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
   } else if (tid >= 32 && tid < 48) {
     const int m = tid - 32;
     S.cohf[m] = P->cohesion > 0.0f && m <= 8 ? 1.0f + P->cohesion * (float)m : 1.0f;
+  } else if (tid >= 64 && tid < 72) {
+    // expected decays of a channel with min(act, 8) = m activated monomers
+    // (transport.wgsl:281-287): the step's constants, the same operations
+    const uint32_t m = (uint32_t)(tid - 63);
+    const float shield = 1.0f / (1.0f + CHEM_SHIELD * (float)(m - 1u));
+    S.exp_dec[m - 1] = (float)m * rb_max(P->activation_decay, 0.0f) * shield *
+                       (float)(P->transport_every > 1u ? P->transport_every : 1u);
   }
   __syncthreads();
 
@@ -595,6 +604,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       }
       // local reactions per channel (transport.wgsl:262-294)
       const uint32_t words[4] = {cw.x, cw.y, cw.z, cw.w};
+      const float light_term = LIGHT_ACT_P * rb_max(P->uv_strength, 0.0f) * rb_max(P->direct_photoactivation, 0.0f) * light_t;
 #pragma unroll
       for (uint32_t ch = 0; ch < 4; ch++) {
         const uint32_t slot = (uint32_t)(idx * 4 + ch);
@@ -602,22 +612,21 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         uint32_t spent_n = words[ch] >> 16;
         S.segw[ch][tid] = 0u;
         if (act_n + spent_n == 0u) continue;
+        // rb_pcg4d(slot, epoch, RB_S_PHOTO / RB_S_DECAY, seed), sharing the slot's head
+        const st::PcgHead rh = st::pcg_head(slot, P->epoch, P->seed);
         if (spent_n > 0u) {
           float sens = 1.0f + CHEM_SENSITIZE * (float)umin(act_n, 8u);
-          float exp_act = (float)umin(spent_n, 8u) * tn *
-                          (LIGHT_ACT_P * rb_max(P->uv_strength, 0.0f) * rb_max(P->direct_photoactivation, 0.0f) * light_t * sens +
-                           rb_max(P->reactivation_rate, 0.0f));
+          float exp_act = (float)umin(spent_n, 8u) * tn * (light_term * sens + rb_max(P->reactivation_rate, 0.0f));
           uint32_t na = rb_f2u(rb_floor(exp_act));
           float frac = exp_act - (float)na;
-          if (frac > 0.0f && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_PHOTO, P->seed).x) < frac) na += 1u;
+          if (frac > 0.0f && rb_u2f(st::pcg_draw(rh, st::pcg_z0(RB_S_PHOTO)).x) < frac) na += 1u;
           na = umin(na, umin(spent_n, 8u));
           act_n += na;
           spent_n -= na;
         }
         if (act_n > 0u) {
-          float shield = 1.0f / (1.0f + CHEM_SHIELD * (float)(umin(act_n, 8u) - 1u));
-          float exp_dec = (float)umin(act_n, 8u) * rb_max(P->activation_decay, 0.0f) * shield * tn;
-          if (exp_dec > 0.0f && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_DECAY, P->seed).x) < exp_dec) {
+          const float exp_dec = S.exp_dec[umin(act_n, 8u) - 1u];
+          if (exp_dec > 0.0f && rb_u2f(st::pcg_draw(rh, st::pcg_z0(RB_S_DECAY)).x) < exp_dec) {
             act_n -= 1u;
             spent_n += 1u;
           }
@@ -626,7 +635,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         const uint32_t movers = umin(n, MAX_MOVERS_PER_CH);
         const uint32_t act_stay = act_n - umin(act_n, movers);
         const uint32_t stay = act_stay + (n - movers - act_stay) * CHEM_SPENT_ONE;
-        if (stay) atomicAdd(&S.accum[say * st::AW + sax][ch], stay);
+        if (stay) atomicAdd(&S.accum[ch][say * st::AW + sax], stay);
         S.segw[ch][tid] = umin(act_n, st::ACT_MASK) | (act_n > 0u ? nbm[ch] << st::ACT_BITS : 0u);
         mov[ch] = movers;
       }
@@ -742,7 +751,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       const uint32_t bi = (uint32_t)iclamp(offy, 0, 3) * 4u + (uint32_t)iclamp(offx, 0, 3);
       const uint16_t sl = S.slot[bi][ct];
       if (sl != st::FAR) {
-        atomicAdd(&S.accum[sl][ch], unit);
+        atomicAdd(&S.accum[ch][sl], unit);
       } else {
         int tx = iclamp(cx + basex + (int)(bi & 3u), 0, (int)G - 1);
         int ty = iclamp(cy + basey + (int)(bi >> 2), 0, (int)GH - 1);
@@ -755,7 +764,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
   // ---- C. accumulator -> chem_next ----
   for (int e = tid; e < st::AC * 4; e += st::NT) {
     int cell = e >> 2, ch = e & 3;
-    uint32_t v = S.accum[cell][ch];
+    uint32_t v = S.accum[ch][cell];
     if (!v) continue;
     int gx = X0 - st::HALO + cell % st::AW, gy = Y0 - st::HALO + cell / st::AW;
     atomicAdd(d.chem_next + ((size_t)gy * G + gx) * 4 + ch, v);
