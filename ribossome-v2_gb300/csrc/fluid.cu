@@ -249,6 +249,11 @@ __global__ void k_advect(const __grid_constant__ S s, int dir) {
   RB_WORLD(s);
   const float2* __restrict__ vin = dir ? d.vb : d.va;
   float2* __restrict__ vout = dir ? d.va : d.vb;
+  // the step's decay factor, one evaluation per CTA (every thread would
+  // compute the same value)
+  __shared__ float decay_shared;
+  if (threadIdx.x == 0 && threadIdx.y == 0) decay_shared = rb_pow(rb_clamp(P->fluid_decay, 0.0f, 1.0f), fluid_dt(P) * 60.0f);
+  __syncthreads();
   uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
@@ -257,14 +262,14 @@ __global__ void k_advect(const __grid_constant__ S s, int dir) {
     return;
   }
   const float dt = fluid_dt(P);
-  const float decay_factor = rb_pow(rb_clamp(P->fluid_decay, 0.0f, 1.0f), dt * 60.0f);
+  const float decay_factor = decay_shared;
   const float2 n = d.normal[idx];
   float2 pos = f2((float)x + 0.5f, (float)y + 0.5f);
-  float2 vel = reflect_n(n, clamp_len(raw_velocity_cell(d, vin, x, y), MAX_VEL));
+  float2 vel = reflect_stored(n, clamp_len(raw_velocity_cell(d, vin, x, y), MAX_VEL));
   float2 trace_pos = sub2(pos, mul2(vel, dt));
-  if (is_solid_at_pos(d, trace_pos)) trace_pos = sub2(pos, mul2(reflect_n(n, vel), dt));
+  if (is_solid_at_pos(d, trace_pos)) trace_pos = sub2(pos, mul2(reflect_stored(n, vel), dt));
   float2 out_v = sanitize(mul2(sample_velocity(d, vin, trace_pos), decay_factor));
-  out_v = reflect_n(n, out_v);
+  out_v = reflect_stored(n, out_v);
   vout[idx] = clamp_len(out_v, MAX_VEL);
 }
 

@@ -171,6 +171,11 @@ __device__ __forceinline__ size_t env_cell_for_fluid(const Dev& d, uint32_t x, u
   uint32_t gy = rb_f2u(rb_clamp(((float)y + 0.5f) * d.sy, 0.0f, (float)(d.gh - 1)));
   return (size_t)gy * d.gw + gx;
 }
+// min(g, GAMMA_SOLID) / GAMMA_SOLID for g = 0..GAMMA_SOLID: the quotients the
+// fill sum adds, divided once at compile time (IEEE division either way).
+__constant__ const float FILL_TERM[4] = {0.0f / (float)GAMMA_SOLID, 1.0f / (float)GAMMA_SOLID,
+                                         2.0f / (float)GAMMA_SOLID, 3.0f / (float)GAMMA_SOLID};
+static_assert(GAMMA_SOLID == 3u, "FILL_TERM lists the quotients for GAMMA_SOLID = 3");
 // fluid.wgsl:114-128
 __device__ __forceinline__ float gamma_fill_at_fluid_cell(const Dev& d, uint32_t x, uint32_t y) {
   float gx = ((float)x + 0.5f) * d.sx, gy = ((float)y + 0.5f) * d.sy;
@@ -182,7 +187,7 @@ __device__ __forceinline__ float gamma_fill_at_fluid_cell(const Dev& d, uint32_t
     float oy = (s & 2u) == 2u ? hy : -hy;
     uint32_t sx = rb_f2u(rb_clamp(gx + ox, 0.0f, (float)(d.gw - 1)));
     uint32_t sy = rb_f2u(rb_clamp(gy + oy, 0.0f, (float)(d.gh - 1)));
-    fill += (float)umin(__ldg(d.gamma + (size_t)sy * d.gw + sx), GAMMA_SOLID) / (float)GAMMA_SOLID;
+    fill += FILL_TERM[umin(__ldg(d.gamma + (size_t)sy * d.gw + sx), GAMMA_SOLID)];
   }
   return fill * 0.25f;
 }
@@ -217,17 +222,24 @@ __device__ __forceinline__ float2 reflect_n(float2 n, float2 v_in) {
 // The wall normal depends on the mask alone, so it is computed once per
 // mask build (k_wall_normals) and read here: same function, same bits.  A
 // stored normal is either exactly (0, 0) or of length about 1 (solid_normal
-// divides by a length above 1e-6), so "length > 1e-6" is "not (0, 0)".
-__device__ __forceinline__ float2 reflect_if_into_solid(const Dev& d, uint32_t x, uint32_t y, float2 v) {
-  const float2 n = d.normal[(size_t)y * d.fw + x];
+// divides by a length above 1e-6), so reflect_n's "length > 1e-6" is
+// "not (0, 0)" for it.
+__device__ __forceinline__ float2 reflect_stored(float2 n, float2 v) {
   if (n.x == 0.0f && n.y == 0.0f) return v;
   const float dd = dot2(v, n);
   return dd < 0.0f ? sub2(v, mul2(n, dd)) : v;
 }
+__device__ __forceinline__ float2 reflect_if_into_solid(const Dev& d, uint32_t x, uint32_t y, float2 v) {
+  return reflect_stored(d.normal[(size_t)y * d.fw + x], v);
+}
 // fluid.wgsl:191-194 on an arbitrary input buffer
+// Both loads are issued unconditionally (the cell is in the grid), so they
+// overlap instead of the velocity load waiting on the mask.
 __device__ __forceinline__ float2 raw_velocity_cell(const Dev& d, const float2* vin, uint32_t x, uint32_t y) {
-  if (is_solid(d, x, y)) return f2(0.0f, 0.0f);
-  return sanitize(vin[(size_t)y * d.fw + x]);
+  const size_t i = (size_t)y * d.fw + x;
+  const uint8_t solid = d.mask[i];
+  const float2 v = vin[i];
+  return solid ? f2(0.0f, 0.0f) : sanitize(v);
 }
 
 // ---- light helpers used by the temperature pass (light.wgsl:46-102,182-189) ----
