@@ -350,6 +350,7 @@ struct Smem {
   float4 press[NT];                // osmotic hop weights (+x, -x, +y, -y)
   float acc[8][NT];                // Kawasaki acceptance per direction: activated 0-3, spent 4-7
   uint32_t segw[4][NT];            // per channel: activated count | neighbour counts (above)
+  uint32_t head[4][NT];            // per channel: hash head (x1) of the cell-channel slot
   uint16_t slot[16][NT];           // accumulator slot of each window bin (blocking resolved), or FAR
   uint32_t off[TY][4 * TX + 1];    // per warp: exclusive prefix of movers over (cell, channel)
   uint32_t accum[4][AC];           // tile + ring destination sums [channel][cell] (lanes on
@@ -614,6 +615,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         if (act_n + spent_n == 0u) continue;
         // rb_pcg4d(slot, epoch, RB_S_PHOTO / RB_S_DECAY, seed), sharing the slot's head
         const st::PcgHead rh = st::pcg_head(slot, P->epoch, P->seed);
+        S.head[ch][tid] = rh.x1;
         if (spent_n > 0u) {
           float sens = 1.0f + CHEM_SENSITIZE * (float)umin(act_n, 8u);
           float exp_act = (float)umin(spent_n, 8u) * tn * (light_term * sens + rb_max(P->reactivation_rate, 0.0f));
@@ -682,7 +684,9 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
     int cx = X0 + c;
     const uint32_t epoch = P->epoch, seed = P->seed;
     // per segment: the hash head of its slot, the cell's mover parameters
-    st::PcgHead ph = st::pcg_head((uint32_t)(((size_t)cy * G + cx) * 4 + ch), epoch, seed);
+    // the slot's hash head, left by the per-cell part (y0, w0 are the step's)
+    st::PcgHead ph = st::pcg_head(0u, epoch, seed);
+    ph.x1 = S.head[ch][ct];
     uint32_t segw = S.segw[ch][ct];
     float4 mv0 = S.mv0[ct], mv1 = S.mv1[ct];
     int basex = rb_floor_i(mv0.x) - 1, basey = rb_floor_i(mv0.y) - 1;
@@ -701,7 +705,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         ch = s & 3;
         ct = warp * 32 + c;
         cx = X0 + c;
-        ph = st::pcg_head((uint32_t)(((size_t)cy * G + cx) * 4 + ch), epoch, seed);
+        ph.x1 = S.head[ch][ct];
         segw = S.segw[ch][ct];
         mv0 = S.mv0[ct];
         mv1 = S.mv1[ct];
