@@ -481,6 +481,37 @@ ribo_status ribo_pressure_solve_noalloc(uint32_t fluid_w, uint32_t fluid_h, cons
                                         uint32_t mg_pre, uint32_t mg_post, uint32_t mg_coarse, uint32_t mg_cycles,
                                         void* cuda_stream);
 
+// Scene files: World::save_scene / Scene::read + World::load_scene
+// (src/world/snapshot.rs:274-368, 145-167, 372-553) for the world blocks of
+// this path.  The file is the reference's `.ribo` container ("RIBOSCN1", JSON
+// header, LZ4 blocks): the header's cfg, params (SimParams by field name) and
+// settings, the blocks chem, gamma, velocity, pressure, temperature and
+// redox, zero agents (empty agent blocks, so the reference can load the
+// file into a world of the same size), and this path's frozen inputs (vent
+// heat, light, shade) as extra blocks the reference ignores.  save waits for
+// the world's stream and writes `path` through a temporary file.  load
+// accepts the reference's scenes: the sizes must match this world's
+// (RIBO_INVALID_ARG otherwise), unknown parameter names are ignored and
+// missing ones take the defaults (ribo_sim_params_default); it uploads the
+// blocks (gamma first: slope and wall mask are rebuilt), sets the world's
+// settings from the header, fills `params` (may be null) and leaves the
+// fields the file lacks (e.g. light and heat of a reference scene) as they
+// were.
+ribo_status ribo_world_save_scene(ribo_world* w, const char* path, const ribo_sim_params* params);
+ribo_status ribo_world_load_scene(ribo_world* w, const char* path, ribo_sim_params* params);
+
+// SimParams field `i` (0..115) by the reference's name (src/params.rs:71-81,
+// the names of to_named / set_named), or NULL past the last.
+const char* ribo_sim_param_name(uint32_t i);
+
+// The LZ4 block coder of the scene files (published LZ4 block format, the
+// blocks lz4_flex's compress_prepend_size writes after its 4-byte length).
+// compress writes at most ribo_lz4_compress_bound(n) bytes; decompress
+// fails with RIBO_INVALID_ARG on malformed input or a short output buffer.
+size_t ribo_lz4_compress_bound(size_t n);
+ribo_status ribo_lz4_compress(const void* src, size_t n, void* dst, size_t cap, size_t* written);
+ribo_status ribo_lz4_decompress(const void* src, size_t n, void* dst, size_t cap, size_t* written);
+
 #ifdef __cplusplus
 }  // extern "C"
 #endif

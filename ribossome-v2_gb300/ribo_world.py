@@ -143,6 +143,12 @@ def load_library(path: str = LIB_PATH):
         "ribo_world_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "ribo_world_read_kernel_timing": ([vp, P(KernelTiming), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_kernel_launch_count": ([], ctypes.c_uint64),
+        "ribo_world_save_scene": ([vp, ctypes.c_char_p, P(SimParams)], ctypes.c_int),
+        "ribo_world_load_scene": ([vp, ctypes.c_char_p, P(SimParams)], ctypes.c_int),
+        "ribo_sim_param_name": ([ctypes.c_uint32], ctypes.c_char_p),
+        "ribo_lz4_compress_bound": ([ctypes.c_size_t], ctypes.c_size_t),
+        "ribo_lz4_compress": ([vp, ctypes.c_size_t, vp, ctypes.c_size_t, P(ctypes.c_size_t)], ctypes.c_int),
+        "ribo_lz4_decompress": ([vp, ctypes.c_size_t, vp, ctypes.c_size_t, P(ctypes.c_size_t)], ctypes.c_int),
         "ribo_world_step_ledgers": ([vp, P(ctypes.c_uint32), ctypes.c_uint32], ctypes.c_int),
         "ribo_world_mark": ([vp, ctypes.c_uint32], ctypes.c_int),
         "ribo_world_elapsed_ms": ([vp, ctypes.c_uint32, ctypes.c_uint32, P(ctypes.c_float)], ctypes.c_int),
@@ -190,6 +196,39 @@ def check(status: int, what: str = ""):
 
 def kernel_launch_count() -> int:
     return int(load_library().ribo_kernel_launch_count())
+
+
+def sim_param_names():
+    """SimParams field names in order (the reference's to_named names)."""
+    lib = load_library()
+    out, i = [], 0
+    while True:
+        n = lib.ribo_sim_param_name(i)
+        if n is None:
+            return out
+        out.append(n.decode())
+        i += 1
+
+
+def lz4_compress(data: bytes) -> bytes:
+    """One LZ4 block (the scene files' block coder)."""
+    lib = load_library()
+    src = bytes(data)
+    cap = lib.ribo_lz4_compress_bound(len(src))
+    dst = ctypes.create_string_buffer(max(cap, 1))
+    n = ctypes.c_size_t()
+    check(lib.ribo_lz4_compress(src, len(src), dst, cap, ctypes.byref(n)), "lz4_compress")
+    return dst.raw[:n.value]
+
+
+def lz4_decompress(block: bytes, size: int) -> bytes:
+    """Decodes one LZ4 block of `size` bytes."""
+    lib = load_library()
+    src = bytes(block)
+    dst = ctypes.create_string_buffer(max(size, 1))
+    n = ctypes.c_size_t()
+    check(lib.ribo_lz4_decompress(src, len(src), dst, size, ctypes.byref(n)), "lz4_decompress")
+    return dst.raw[:n.value]
 
 
 def default_params(seed: int = 1) -> SimParams:
@@ -388,6 +427,19 @@ class World:
         out = (ctypes.c_uint32 * 12)()
         check(self._lib.ribo_world_ledger(self._h, out), "ledger")
         return Ledger.from_words(out)
+
+    # ---- scenes (src/world/snapshot.rs) ----
+    def save_scene(self, path: str):
+        """Writes the world (blocks, params, settings) as a .ribo scene file."""
+        self._sync_settings()
+        check(self._lib.ribo_world_save_scene(self._h, os.fsencode(path), ctypes.byref(self.params)), "save_scene")
+
+    def load_scene(self, path: str):
+        """Loads a .ribo scene of this world's size: blocks, params and settings."""
+        p = SimParams()
+        check(self._lib.ribo_world_load_scene(self._h, os.fsencode(path), ctypes.byref(p)), "load_scene")
+        self.params = p
+        check(self._lib.ribo_world_get_settings(self._h, ctypes.byref(self.settings)), "get_settings")
 
     def seed_inputs(self, inputs: dict):
         """Uploads a dict {field: array} (e.g. from synth.make_world_inputs)."""
