@@ -196,6 +196,12 @@ typedef struct ribo_world_settings {
   uint32_t mixed_max_outer;   // defect-correction steps at most [4]
   uint32_t mixed_max_inner;   // conjugate-gradient iterations per step at most [64]
   float mixed_alpha;          // over-relaxation of the V-cycle's coarse correction [1.8]
+  // UV light (shaders/world/light.wgsl, src/world/mod.rs:1505-1524):
+  uint32_t light_mode;           // 0 = the LIGHT field is a frozen input [default]; 1 = the reference's light
+                                 // block runs before the fluid block of every step
+  uint32_t light_rows_per_step;  // light_mode 1: rows the light propagates per step (at most 16); 0 = a full
+                                 // sweep every light_interval steps [1]
+  uint32_t light_interval;       // steps between full sweeps when light_rows_per_step = 0 [10]
 } ribo_world_settings;
 
 // Device fields a caller can upload / read.  Sizes in bytes, for a world with

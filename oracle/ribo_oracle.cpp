@@ -118,6 +118,8 @@ struct Oracle {
   int gw, gh, fw, fh, lw, lh, rx, ry;
   float sim_w, sim_h;
   bool fluid_was_on = true;
+  bool light_dirty = true;        // the next light block is a full sweep
+  std::vector<float> light_next;  // light_propagate's output
   const ribo_sim_params* P = nullptr;
 
   std::vector<uint32_t> chem, chem_next, gamma, agg_act, agg_nb, shade, force_vec, redox_eaten, solid_mask;
@@ -344,6 +346,63 @@ struct Oracle {
     incoming = rb_max(incoming, 0.0f);
     return incoming * ((1.0f - light_transmit(lx, ly, 0u)) + SUN_WATER_ABSORB);
   }
+  // ---- the light block (light.wgsl:43-45, 141-177; src/world/mod.rs:1505-1524) ----
+  float row_water(uint32_t band) const {
+    return rb_exp(-rb_max(P->uv_depth, 0.0f) * (band == 1u ? (float)0.03 : 1.0f) * (float)LIGHT_DIV / (float)gh);
+  }
+  void light_transmit_pass() {
+    const size_t L = lcells();
+    std::vector<float> t0(L), t1(L);  // every transmission reads chem, gamma and shade only
+    for (int y = 0; y < lh; y++)
+      for (int x = 0; x < lw; x++) {
+        t0[(size_t)y * lw + x] = light_transmit(x, y, 0u);
+        t1[(size_t)y * lw + x] = light_transmit(x, y, 1u);
+      }
+    std::copy(t0.begin(), t0.end(), light.begin());
+    std::copy(t1.begin(), t1.end(), light.begin() + L);
+  }
+  void compute_uv_light() {
+    const size_t L = lcells();
+    const uint32_t top = (uint32_t)lh - 1u;
+    const float w0 = row_water(0u), w1 = row_water(1u);
+    for (int x = 0; x < lw; x++) {
+      light[(size_t)top * lw + x] *= w0 * P->sun_now;
+      light[L + (size_t)top * lw + x] *= w1 * P->sun_now;
+    }
+    for (uint32_t t = 1; t < (uint32_t)lh; t++) {
+      const uint32_t y = (uint32_t)lh - 1u - t;
+      for (int x = 0; x < lw; x++) {
+        const float a0 = light_above(x, y + 1u, 0u), a1 = light_above(x, y + 1u, 1u);
+        light[(size_t)y * lw + x] *= a0 * w0;
+        light[L + (size_t)y * lw + x] *= a1 * w1;
+      }
+    }
+  }
+  void light_propagate() {
+    const size_t L = lcells();
+    for (int y = 0; y < lh; y++)
+      for (int x = 0; x < lw; x++)
+        for (uint32_t band = 0; band < 2u; band++) {
+          float above = P->sun_now;
+          if ((uint32_t)y + 1u < (uint32_t)lh) above = light_above(x, y + 1u, band);
+          light_next[band * L + (size_t)y * lw + x] = above * row_water(band) * light_transmit(x, y, band);
+        }
+  }
+  void light_commit() { light = light_next; }
+  void light_block(uint32_t epoch) {
+    const uint32_t interval = std::max(st.light_interval, 1u);
+    if (light_dirty || (st.light_rows_per_step == 0u && epoch % interval == 0u)) {
+      light_dirty = false;
+      light_transmit_pass();
+      compute_uv_light();
+    } else {
+      for (uint32_t r = 0; r < std::min(st.light_rows_per_step, 16u); r++) {
+        light_propagate();
+        light_commit();
+      }
+    }
+  }
+
   float uv_light_at_cell(uint32_t x, uint32_t y) const {
     uint32_t lx = std::min(x, (uint32_t)gw - 1u) / LIGHT_DIV;
     uint32_t ly = std::min(y, (uint32_t)gh - 1u) / LIGHT_DIV;
@@ -1154,6 +1213,7 @@ struct Oracle {
     P = p;
     uint32_t epoch = p->epoch;
     uint32_t substep = std::min(std::max(st.fluid_substep, 1u), 4u);
+    if (st.light_mode) light_block(epoch);
     if (st.fluid_enabled && epoch % substep == 0u) {
       build_solid_mask();
       update_temperature();
@@ -1245,6 +1305,7 @@ void* orc_create(const ribo_world_cfg* cfg) {
   o->redox_eaten.assign(F, 0);
   o->solid_mask.assign(F, 0);
   o->light.assign(2 * L, 0.0f);
+  o->light_next.assign(2 * L, 0.0f);
   o->pressure_a.assign(F, 0.0f);
   o->pressure_b.assign(F, 0.0f);
   o->div.assign(F, 0.0f);
@@ -1265,7 +1326,11 @@ void* orc_create(const ribo_world_cfg* cfg) {
 
 void orc_destroy(void* w) { delete (Oracle*)w; }
 
-void orc_set_settings(void* w, const ribo_world_settings* s) { ((Oracle*)w)->st = *s; }
+void orc_set_settings(void* w, const ribo_world_settings* s) {
+  Oracle* o = (Oracle*)w;
+  if (s->light_mode && !o->st.light_mode) o->light_dirty = true;
+  o->st = *s;
+}
 
 int orc_upload(void* w, int field, const void* host, size_t bytes) {
   Oracle* o = (Oracle*)w;
@@ -1278,6 +1343,7 @@ int orc_upload(void* w, int field, const void* host, size_t bytes) {
     // rebuilds the mask at every fluid step, as the reference does.
     o->compute_slope();
     o->build_solid_mask();
+    o->light_dirty = true;
   }
   return 0;
 }

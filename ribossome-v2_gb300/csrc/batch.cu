@@ -45,6 +45,10 @@ void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby) {
       *nbx = (d.fh + NET_FLUX_LINES - 1) / NET_FLUX_LINES + (d.fw + NET_FLUX_LINES - 1) / NET_FLUX_LINES;
       *nby = 1;
       return;
+    case GEO_LIGHT:
+      *nbx = (d.lw + PASS_BX - 1) / PASS_BX;
+      *nby = (d.lh + PASS_BY - 1) / PASS_BY;
+      return;
     case GEO_LEDGER: {
       long long b = (cells + LEDGER_CELLS_PER_CTA - 1) / LEDGER_CELLS_PER_CTA;
       *nbx = (int)(b < 1 ? 1 : (b > 152 * 8 ? 152 * 8 : b));
@@ -491,6 +495,9 @@ ribo_status Batch::step(const ribo_sim_params* per_step, uint32_t n, const uint3
   if (member_steps)
     for (size_t k = 0; k < worlds.size(); k++)
       if (member_steps[k] > n) return set_error(RIBO_INVALID_ARG, "member %zu: %u steps of %u", k, member_steps[k], n);
+  for (size_t k = 0; k < worlds.size(); k++)
+    if (worlds[k]->st.light_mode)
+      return set_error(RIBO_INVALID_ARG, "member %zu: batches take worlds whose light is a frozen input (light_mode 0)", k);
   RB_TRY(bind(), "device");
   {
     ribo_status s = ensure_capacity();

@@ -81,6 +81,7 @@ struct Dev {
   uint32_t* chem_next;  // transport destination (zero between steps)
   const uint32_t* gamma;
   const float* light;
+  float* light_next;  // light_propagate's output (the light block; the light field itself is written through light)
   const uint32_t* shade;
   float2* slope;
   uint32_t* agg_act;

@@ -30,6 +30,7 @@ enum Geo : int {
   GEO_SCATTER,      // environment grid, SCATTER_TX x SCATTER_TY tiles
   GEO_NET_FLUX,     // fluid rows then columns, NET_FLUX_LINES per CTA (1-D)
   GEO_LEDGER,       // environment cells, LEDGER_CELLS_PER_CTA per CTA (1-D)
+  GEO_LIGHT,        // light grid (grid / LIGHT_DIV), PASS_BX x PASS_BY cells per CTA
   GEO_COUNT
 };
 void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby);
@@ -73,6 +74,12 @@ Target target_one(const Dev& d, const ribo_sim_params* P);
 // Velocity ping-pong direction of a pass: reads velocity_a, writes
 // velocity_b (A_TO_B) or the reverse (B_TO_A).
 enum : int { A_TO_B = 0, B_TO_A = 1 };
+
+// light.cu (light_mode 1)
+void launch_light_transmit(const Target& t, cudaStream_t s);
+void launch_light_sweep(const Dev& d, const ribo_sim_params* P, cudaStream_t s);
+void launch_light_propagate(const Target& t, cudaStream_t s);
+void launch_light_commit(const Target& t, cudaStream_t s);
 
 // fluid.cu
 void launch_solid_mask(const Target& t, cudaStream_t s);

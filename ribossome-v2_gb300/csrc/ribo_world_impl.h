@@ -74,6 +74,8 @@ struct World {
   uint32_t *chem_a = nullptr, *chem_b = nullptr, *chem_cur = nullptr, *chem_nxt = nullptr;
   uint32_t* gamma = nullptr;
   float* light = nullptr;
+  float* light_next = nullptr;  // light_propagate's output (light_mode 1)
+  bool light_dirty = true;      // the next light block is a full sweep (creation, gamma upload, light turned on)
   uint32_t* shade = nullptr;
   float2* slope = nullptr;
   uint32_t *agg_act = nullptr, *agg_nb = nullptr;
@@ -134,6 +136,9 @@ struct World {
   ribo_status record_steps_graphed(const ribo_sim_params* per_step, const ribo_sim_params* ds, uint32_t n, int slot);
   ribo_status read_timing(ribo_kernel_timing* out, uint32_t cap, uint32_t* count);
   void record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uint32_t i);
+  // light_mode 1: whether the light block of a step with these parameters is
+  // a full sweep (else rows of propagation), given the dirty flag before it
+  bool light_sweeps(const ribo_sim_params& hp, bool dirty) const;
   cudaError_t bind() const;
   void pressure_solve(const Dev& d);
 };

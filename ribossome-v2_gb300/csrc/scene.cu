@@ -597,7 +597,8 @@ const SettingField SETTINGS[] = {RB_SETTING(fluid_enabled),  RB_SETTING(fluid_su
                                  RB_SETTING(mg_cycles),      RB_SETTING(jacobi_iters),    RB_SETTING(ledger_each_step),
                                  RB_SETTING(mg_unfused),     RB_SETTING(transport_simple), RB_SETTING(mixed_tol),
                                  RB_SETTING(mixed_inner_tol), RB_SETTING(mixed_max_outer), RB_SETTING(mixed_max_inner),
-                                 RB_SETTING(mixed_alpha)};
+                                 RB_SETTING(mixed_alpha),    RB_SETTING(light_mode),      RB_SETTING(light_rows_per_step),
+                                 RB_SETTING(light_interval)};
 #undef RB_SETTING
 static_assert(sizeof(SETTINGS) / sizeof(SETTINGS[0]) * 4 == sizeof(ribo_world_settings), "every setting is named");
 
@@ -685,7 +686,8 @@ extern "C" ribo_status ribo_world_save_scene(ribo_world* w, const char* path, co
   h += std::string("{\"fluid_enabled\": ") + (s.fluid_enabled ? "true" : "false") +
        ", \"fluid_substep\": " + fmt_num(s.fluid_substep) + ", \"multigrid\": " + (s.multigrid ? "true" : "false") +
        ", \"mg_cycles\": " + fmt_num(s.mg_cycles) + ", \"jacobi_iters\": " + fmt_num(s.jacobi_iters) +
-       ", \"light_rows_per_step\": 1, \"light_interval\": 10, \"terrain_enabled\": false, \"contact_enabled\": true}";
+       ", \"light_rows_per_step\": " + fmt_num(s.light_rows_per_step) + ", \"light_interval\": " +
+       fmt_num(s.light_interval) + ", \"terrain_enabled\": false, \"contact_enabled\": true}";
   json_key(h, "gb300_settings", first);
   h += "{";
   for (size_t i = 0; i < sizeof(SETTINGS) / sizeof(SETTINGS[0]); i++) {
@@ -810,6 +812,8 @@ extern "C" ribo_status ribo_world_load_scene(ribo_world* w, const char* path, ri
     if (json_number(rs->get("multigrid"), v)) s.multigrid = v != 0.0;
     if (json_number(rs->get("mg_cycles"), v)) s.mg_cycles = (uint32_t)v;
     if (json_number(rs->get("jacobi_iters"), v)) s.jacobi_iters = (uint32_t)v;
+    if (json_number(rs->get("light_rows_per_step"), v)) s.light_rows_per_step = (uint32_t)v;
+    if (json_number(rs->get("light_interval"), v)) s.light_interval = (uint32_t)v;
   }
   if (const Json* gs8 = header.get("gb300_settings")) {
     for (const SettingField& f : SETTINGS) {

@@ -165,6 +165,7 @@ Dev World::dev() const {
   d.chem_next = chem_nxt;
   d.gamma = gamma;
   d.light = light;
+  d.light_next = light_next;
   d.shade = shade;
   d.slope = slope;
   d.agg_act = agg_act;
@@ -246,7 +247,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   const size_t M = build_levels((int)c.fluid_w, (int)c.fluid_h, c.mg_min_size ? c.mg_min_size : 8, lv);
   size_t b = 0;
   b += C * (16 + 16 + 4 + 8 + 4 + 4);                             // chem a/b, gamma, slope, agg_act, agg_nb
-  b += 2 * L * 4 * 2;                                             // light, shade
+  b += 2 * L * 4 * 3;                                             // light, light_next, shade
   b += F * (1 + 8 + 4 + 8 * 3 + 4 * 3 + 4 * 5 + 8 * 3 + 4 + 4);  // mask..heat, mask32, p_tmp
   b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 + MAX_STEPS * 12 * 4 + 16;
   b += M * (4 + 4 + 1 + 4);                                       // mg p, rhs, fluid, p2
@@ -280,6 +281,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(gamma, C * 4);
   RB_ALLOC(light, 2 * L * 4);
   RB_ALLOC(shade, 2 * L * 4);
+  RB_ALLOC(light_next, 2 * L * 4);
   RB_ALLOC(slope, C * 8);
   RB_ALLOC(agg_act, C * 4);
   RB_ALLOC(agg_nb, C * 4);
@@ -376,6 +378,7 @@ ribo_status World::upload(ribo_field f, const void* host, size_t bytes) {
     RB_TRY(cudaGetLastError(), "slope/mask");
     ribo_status ms = mixed_setup(*this);
     if (ms != RIBO_OK) return ms;
+    light_dirty = true;  // the terrain changed: the next light block sweeps
   }
   RB_TRY(cudaStreamSynchronize(stream), "upload");
   return RIBO_OK;
@@ -431,8 +434,29 @@ void World::pressure_solve(const Dev& d) {
   }
 }
 
-// The fluid and transport blocks of one step (src/world/mod.rs:1527-1601).
+// src/world/mod.rs:1506: a full sweep when the light is dirty or, without
+// propagation, every light_interval steps.
+bool World::light_sweeps(const ribo_sim_params& hp, bool dirty) const {
+  const uint32_t interval = st.light_interval < 1 ? 1 : st.light_interval;
+  return dirty || (st.light_rows_per_step == 0 && hp.epoch % interval == 0u);
+}
+
+// The light, fluid and transport blocks of one step (src/world/mod.rs:1505-1601).
 void World::record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uint32_t i) {
+  if (st.light_mode) {
+    const Target t = target_one(dev(), P);
+    if (light_sweeps(hp, light_dirty)) {
+      light_dirty = false;
+      launch_light_transmit(t, stream);
+      launch_light_sweep(dev(), P, stream);
+    } else {
+      const uint32_t rows = st.light_rows_per_step > 16 ? 16 : st.light_rows_per_step;
+      for (uint32_t r = 0; r < rows; r++) {
+        launch_light_propagate(t, stream);
+        launch_light_commit(t, stream);
+      }
+    }
+  }
   uint32_t substep = st.fluid_substep < 1 ? 1 : (st.fluid_substep > 4 ? 4 : st.fluid_substep);
   if (st.fluid_enabled && hp.epoch % substep == 0u) {
     launch_temperature(target_one(dev(), P), stream);  // temp_in -> temp_out
@@ -524,11 +548,14 @@ std::string World::graph_key(const ribo_sim_params* per_step, uint32_t n, int sl
   put(&temp_cur, sizeof(void*));
   put(&redox_cur, sizeof(void*));
   uint32_t substep = st.fluid_substep < 1 ? 1 : (st.fluid_substep > 4 ? 4 : st.fluid_substep);
+  bool dirty = light_dirty;
   for (uint32_t i = 0; i < n; i++) {
     const ribo_sim_params& p = per_step[i];
     uint32_t te = p.transport_every < 1 ? 1 : p.transport_every;
+    const bool sweep = st.light_mode && light_sweeps(p, dirty);
+    if (sweep) dirty = false;
     char c = (char)((st.fluid_enabled && p.epoch % substep == 0u ? 1 : 0) | (p.epoch % te == 0u ? 2 : 0) |
-                    (p.aggregation > 0.0f ? 4 : 0));
+                    (p.aggregation > 0.0f ? 4 : 0) | (sweep ? 8 : 0));
     k.push_back(c);
   }
   return k;
@@ -549,6 +576,8 @@ ribo_status World::record_steps_graphed(const ribo_sim_params* per_step, const r
     temp_nxt = g.temp_end == temp_a ? temp_b : temp_a;
     redox_cur = g.redox_end;
     redox_nxt = g.redox_end == redox_a ? redox_b : redox_a;
+    for (uint32_t i = 0; i < n && st.light_mode; i++)
+      if (light_sweeps(per_step[i], light_dirty)) light_dirty = false;
     ktime_add_launches(g.kernels);
     g.uses++;
     return RIBO_OK;
@@ -703,6 +732,8 @@ void ribo_world_settings_default(ribo_world_settings* o) {
   o->mixed_max_outer = 4;
   o->mixed_max_inner = 64;
   o->mixed_alpha = 1.8f;
+  o->light_rows_per_step = 1;  // light_mode 0: the light is a frozen input
+  o->light_interval = 10;
 }
 
 ribo_status ribo_world_solve_info(ribo_world* w, uint32_t* outer, uint32_t* inner, double* rel_residual) {
@@ -761,6 +792,7 @@ void ribo_world_destroy(ribo_world* w) {
 
 ribo_status ribo_world_set_settings(ribo_world* w, const ribo_world_settings* s) {
   if (!w || !s) return set_error(RIBO_INVALID_ARG, "null argument");
+  if (s->light_mode && !w->w.st.light_mode) w->w.light_dirty = true;
   w->w.st = *s;
   return RIBO_OK;
 }

@@ -71,6 +71,7 @@ class WorldSettings(ctypes.Structure):
         ("mg_unfused", ctypes.c_uint32), ("transport_simple", ctypes.c_uint32),
         ("mixed_tol", ctypes.c_float), ("mixed_inner_tol", ctypes.c_float),
         ("mixed_max_outer", ctypes.c_uint32), ("mixed_max_inner", ctypes.c_uint32), ("mixed_alpha", ctypes.c_float),
+        ("light_mode", ctypes.c_uint32), ("light_rows_per_step", ctypes.c_uint32), ("light_interval", ctypes.c_uint32),
     ]
 
 
@@ -102,7 +103,7 @@ class ServerStats(ctypes.Structure):
                 ("world_steps", ctypes.c_uint64), ("iterations", ctypes.c_uint64), ("gpu_ms", ctypes.c_double)]
 
 
-assert ctypes.sizeof(WorldSettings) == 52 and ctypes.sizeof(Job) == 872 and ctypes.sizeof(JobResult) == 104
+assert ctypes.sizeof(WorldSettings) == 64 and ctypes.sizeof(Job) == 880 and ctypes.sizeof(JobResult) == 104
 assert ctypes.sizeof(ServerCfg) == 40
 
 

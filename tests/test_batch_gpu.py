@@ -177,3 +177,16 @@ def test_batch_rejects_bad_arguments(rw):
     b1.close()
     b2.add(w)
     b2.close()
+
+
+def test_batches_reject_the_light_block(rw):
+    import synth
+
+    w = rw.World(64, seed=4)
+    w.seed_inputs(synth.make_world_inputs(64, seed=4))
+    w.settings.light_mode = 1
+    b = rw.Batch()
+    b.add(w)
+    w._sync_settings()
+    with pytest.raises(rw.RiboError, match="frozen input"):
+        b.encode_steps(1)

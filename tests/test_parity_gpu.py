@@ -34,6 +34,13 @@ CASES = [
     ("sparse-transport", 64, None, dict(dt=1.0, transport_every=3, aggregation=0.0), dict(fluid_substep=2), 9, {}),
     ("sun-and-vents", 64, None, dict(dt=0.05, sun_heat=1.0, day_period=400.0, activation_decay=0.01,
                                       direct_photoactivation=0.5), dict(fluid_substep=1), 6, {}),
+    # the light block (light_mode 1): a sweep on the first step, then propagation / interval sweeps
+    ("light-propagate-1-row", 64, None, dict(BASE, direct_photoactivation=0.5), dict(fluid_substep=1, light_mode=1,
+                                                                                   light_rows_per_step=1), 6, {}),
+    ("light-propagate-3-rows-sun", 96, None, dict(dt=0.05, day_period=300.0, sun_heat=1.0, direct_photoactivation=0.5),
+     dict(fluid_substep=1, light_mode=1, light_rows_per_step=3), 6, {}),
+    ("light-interval-sweeps", (128, 64), None, dict(BASE, direct_photoactivation=0.5, monomer_uv_absorb=2.0),
+     dict(fluid_substep=1, light_mode=1, light_rows_per_step=0, light_interval=2), 6, {}),
 ]
 
 
@@ -41,7 +48,7 @@ CASES = [
 def test_steps_bit_exact(rw, ro, case):
     _, grid, fluid, params, settings, steps, mg = case
     g, o, inputs = setup_pair(rw, ro, grid, fluid, params=params, settings=settings, **mg)
-    if case[0] == "sun-and-vents":
+    if case[0] in ("sun-and-vents", "light-propagate-3-rows-sun"):
         rng = np.random.default_rng(3)
         heat = np.zeros(g.field_shape(rw.HEAT)[0], np.float32)
         heat[4:8, 20:24, 0] = 400.0
@@ -161,3 +168,20 @@ def test_deterministic_and_batch_independent(rw):
     assert_same(a[1], b[1], "velocity run-to-run")
     assert_same(a[0], c[0], "cells batched vs single")
     assert_same(a[1], c[1], "velocity batched vs single")
+
+
+def test_light_sweeps_again_after_a_terrain_upload(rw, ro):
+    """Uploading gamma marks the light dirty: the next light block is a full
+    sweep on both sides (src/world/mod.rs:1506)."""
+    g, o, inputs = setup_pair(rw, ro, 64, params=dict(BASE, direct_photoactivation=0.5),
+                              settings=dict(fluid_substep=1, light_mode=1, light_rows_per_step=1))
+    g.encode_steps(3)
+    o.encode_steps(3)
+    gamma = inputs[rw.GAMMA].copy()
+    gamma[20:30, 10:50] = 6
+    g.upload(rw.GAMMA, gamma)
+    o.upload(rw.GAMMA, gamma)
+    g.encode_steps(3)
+    o.encode_steps(3)
+    compare_worlds(g, o, "after the terrain upload")
+    assert_same(g.read(rw.LIGHT), o.read(rw.LIGHT), "light")
