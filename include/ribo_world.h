@@ -287,6 +287,15 @@ ribo_status ribo_derive_step_params(const ribo_sim_params* base, const ribo_worl
 // (held is 0: no agents on this path).  Waits for the world's stream.
 ribo_status ribo_world_ledger(ribo_world* w, uint32_t out[12]);
 
+// Asynchronous ledger (encode_ledger_readback + ledger_after_submit /
+// poll_ledger, src/world/mod.rs:1758-1799): request records the reduction
+// and its copy to pinned host memory on the world's stream, behind the work
+// recorded so far, and returns at once (a request while one is pending does
+// nothing); poll never waits: *ready = 1 and the ledger in `out` once the
+// readback has arrived (the readback is then over), else *ready = 0.
+ribo_status ribo_world_request_ledger(ribo_world* w);
+ribo_status ribo_world_poll_ledger(ribo_world* w, uint32_t out[12], uint32_t* ready);
+
 // With settings.ledger_each_step, the ledger of the state after each step of
 // the last ribo_world_step / encode_steps call (12 words per step, `n` steps
 // of that call).  Waits for the world's stream.

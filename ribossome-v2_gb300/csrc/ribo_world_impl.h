@@ -95,6 +95,11 @@ struct World {
   float* net_flux = nullptr;
   uint32_t* ledger = nullptr;
   uint32_t* step_ledgers = nullptr;  // 64 x 12 words (ledger_each_step)
+  // asynchronous ledger readback (encode_ledger_readback / poll_ledger)
+  uint32_t* ledger_async = nullptr;  // device, 12 words
+  uint32_t* ledger_host = nullptr;   // pinned, 12 words (inside the pinned params block)
+  cudaEvent_t ledger_ev = nullptr;
+  bool ledger_pending = false;
   uint32_t last_steps = 0;
   // multigrid
   std::vector<MgLevel> levels;
@@ -128,6 +133,8 @@ struct World {
   ribo_status read(ribo_field f, void* host, size_t bytes);
   ribo_status step(const ribo_sim_params* per_step, uint32_t n);
   ribo_status ledger_read(uint32_t out[12]);
+  ribo_status ledger_request();
+  ribo_status ledger_poll(uint32_t out[12], uint32_t* ready);
   ribo_status check_status();
   // CUDA-graph replay of repeated step sequences
   std::vector<GraphEntry> graphs;

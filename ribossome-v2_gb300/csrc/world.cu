@@ -249,7 +249,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   b += C * (16 + 16 + 4 + 8 + 4 + 4);                             // chem a/b, gamma, slope, agg_act, agg_nb
   b += 2 * L * 4 * 3;                                             // light, light_next, shade
   b += F * (1 + 8 + 4 + 8 * 3 + 4 * 3 + 4 * 5 + 8 * 3 + 4 + 4);  // mask..heat, mask32, p_tmp
-  b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 + MAX_STEPS * 12 * 4 + 16;
+  b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 * 2 + MAX_STEPS * 12 * 4 + 16;
   b += M * (4 + 4 + 1 + 4);                                       // mg p, rhs, fluid, p2
   b += 2 * MAX_STEPS * sizeof(ribo_sim_params);
   if (c.precision_mode == RIBO_PRECISION_MIXED) b += mixed_footprint(c, lv);
@@ -304,6 +304,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(heat, F * 8);
   RB_ALLOC(net_flux, ((size_t)fw + fh) * 4);
   RB_ALLOC(ledger, 12 * 4);
+  RB_ALLOC(ledger_async, 12 * 4);
   RB_ALLOC(step_ledgers, MAX_STEPS * 12 * 4);
   RB_ALLOC(mask32, F * 4);
   chem_cur = chem_a;
@@ -322,11 +323,13 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(status, 16);
   RB_ALLOC(d_params, 2 * MAX_STEPS * sizeof(ribo_sim_params));
 #undef RB_ALLOC
-  RB_TRY(cudaMallocHost((void**)&h_params, 2 * MAX_STEPS * sizeof(ribo_sim_params)), "pinned params");
+  RB_TRY(cudaMallocHost((void**)&h_params, 2 * MAX_STEPS * sizeof(ribo_sim_params) + 12 * 4), "pinned params");
+  ledger_host = reinterpret_cast<uint32_t*>(h_params + 2 * MAX_STEPS);
   for (int k = 0; k < 2; k++) RB_TRY(cudaEventCreateWithFlags(&param_ev[k], cudaEventDisableTiming), "event");
   RB_TRY(cudaEventCreate(&t0), "event");
   RB_TRY(cudaEventCreate(&t1), "event");
   for (int k = 0; k < 8; k++) RB_TRY(cudaEventCreate(&marks[k]), "event");
+  RB_TRY(cudaEventCreateWithFlags(&ledger_ev, cudaEventDisableTiming), "event");
   if (cfg.precision_mode == RIBO_PRECISION_MIXED) {
     const MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, 1};
     if (!multigrid_fused_ok(levels.data(), (int)levels.size(), c))
@@ -356,6 +359,7 @@ World::~World() {
   if (t1) cudaEventDestroy(t1);
   for (int k = 0; k < 8; k++)
     if (marks[k]) cudaEventDestroy(marks[k]);
+  if (ledger_ev) cudaEventDestroy(ledger_ev);
   if (own_stream) cudaStreamDestroy(own_stream);
 }
 
@@ -658,6 +662,38 @@ ribo_status World::check_status() {
   return RIBO_OK;
 }
 
+// encode_ledger_readback + ledger_after_submit (src/world/mod.rs:1758-1781):
+// the reduction and its copy to pinned memory go on the stream behind the
+// work recorded so far; a request while one is pending does nothing.
+ribo_status World::ledger_request() {
+  if (ledger_pending) return RIBO_OK;
+  RB_TRY(bind(), "device");
+  RB_TRY(cudaMemsetAsync(ledger_async, 0, 12 * sizeof(uint32_t), stream), "ledger");
+  launch_ledger(target_one(dev(), nullptr), ledger_async, stream);
+  RB_TRY(cudaGetLastError(), "ledger");
+  RB_TRY(cudaMemcpyAsync(ledger_host, ledger_async, 12 * 4, cudaMemcpyDeviceToHost, stream), "ledger");
+  RB_TRY(cudaEventRecord(ledger_ev, stream), "ledger");
+  ledger_pending = true;
+  return RIBO_OK;
+}
+
+// poll_ledger (src/world/mod.rs:1783-1799): the ledger once the readback has
+// arrived, else nothing; never waits.
+ribo_status World::ledger_poll(uint32_t out[12], uint32_t* ready) {
+  *ready = 0;
+  if (!ledger_pending) return RIBO_OK;
+  RB_TRY(bind(), "device");
+  const cudaError_t q = cudaEventQuery(ledger_ev);
+  if (q == cudaErrorNotReady) return RIBO_OK;
+  RB_TRY(q, "ledger");
+  ledger_pending = false;
+  ribo_status s = check_status();
+  if (s != RIBO_OK) return s;
+  memcpy(out, ledger_host, 12 * 4);
+  *ready = 1;
+  return RIBO_OK;
+}
+
 ribo_status World::ledger_read(uint32_t out[12]) {
   RB_TRY(bind(), "device");
   RB_TRY(cudaMemsetAsync(ledger, 0, 12 * sizeof(uint32_t), stream), "ledger");
@@ -896,6 +932,16 @@ ribo_status ribo_world_encode_steps(ribo_world* w, ribo_sim_params* params, uint
 ribo_status ribo_world_ledger(ribo_world* w, uint32_t out[12]) {
   if (!w || !out) return set_error(RIBO_INVALID_ARG, "null argument");
   return w->w.ledger_read(out);
+}
+
+ribo_status ribo_world_request_ledger(ribo_world* w) {
+  if (!w) return set_error(RIBO_INVALID_ARG, "null world");
+  return w->w.ledger_request();
+}
+
+ribo_status ribo_world_poll_ledger(ribo_world* w, uint32_t out[12], uint32_t* ready) {
+  if (!w || !out || !ready) return set_error(RIBO_INVALID_ARG, "null argument");
+  return w->w.ledger_poll(out, ready);
 }
 
 ribo_status ribo_world_step_ledgers(ribo_world* w, uint32_t* out, uint32_t n) {

@@ -145,6 +145,8 @@ def load_library(path: str = LIB_PATH):
         "ribo_world_read_kernel_timing": ([vp, P(KernelTiming), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_kernel_launch_count": ([], ctypes.c_uint64),
         "ribo_world_save_scene": ([vp, ctypes.c_char_p, P(SimParams)], ctypes.c_int),
+        "ribo_world_request_ledger": ([vp], ctypes.c_int),
+        "ribo_world_poll_ledger": ([vp, P(ctypes.c_uint32), P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_world_load_scene": ([vp, ctypes.c_char_p, P(SimParams)], ctypes.c_int),
         "ribo_sim_param_name": ([ctypes.c_uint32], ctypes.c_char_p),
         "ribo_lz4_compress_bound": ([ctypes.c_size_t], ctypes.c_size_t),
@@ -423,6 +425,17 @@ class World:
         o, i, r = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
         check(self._lib.ribo_world_solve_info(self._h, ctypes.byref(o), ctypes.byref(i), ctypes.byref(r)), "solve_info")
         return o.value, i.value, r.value
+
+    def request_ledger(self):
+        """encode_ledger_readback: an asynchronous ledger of the state after the work recorded so far."""
+        check(self._lib.ribo_world_request_ledger(self._h), "request_ledger")
+
+    def poll_ledger(self):
+        """poll_ledger: the requested ledger once it has arrived, else None (never waits)."""
+        out = (ctypes.c_uint32 * 12)()
+        ready = ctypes.c_uint32()
+        check(self._lib.ribo_world_poll_ledger(self._h, out, ctypes.byref(ready)), "poll_ledger")
+        return Ledger.from_words(out) if ready.value else None
 
     def ledger_blocking(self) -> Ledger:
         out = (ctypes.c_uint32 * 12)()

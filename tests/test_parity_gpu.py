@@ -185,3 +185,31 @@ def test_light_sweeps_again_after_a_terrain_upload(rw, ro):
     o.encode_steps(3)
     compare_worlds(g, o, "after the terrain upload")
     assert_same(g.read(rw.LIGHT), o.read(rw.LIGHT), "light")
+
+
+def test_async_ledger_readback(rw):
+    """encode_ledger_readback / poll_ledger: the ledger of the state when it
+    was requested, delivered without waiting, one readback at a time."""
+    import time
+
+    import synth
+
+    w = rw.World(128, seed=12)
+    w.seed_inputs(synth.make_world_inputs(128, seed=12))
+    w.params.dt = 1.0
+    w.settings.fluid_substep = 1
+    w.encode_steps(3)
+    assert w.poll_ledger() is None                      # nothing requested
+    want = rw.Ledger.from_cells(w.read_cells_blocking())
+    w.request_ledger()
+    w.request_ledger()                                  # pending: does nothing
+    w.encode_steps(4)                                   # recorded after the request
+    got, t_end = None, time.time() + 30.0
+    while got is None and time.time() < t_end:
+        got = w.poll_ledger()
+    assert got == want
+    assert w.poll_ledger() is None                      # the readback is over
+    w.sync()
+    w.request_ledger()
+    w.sync()
+    assert w.poll_ledger() == w.ledger_blocking()
