@@ -395,6 +395,8 @@ def run_ours(args):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(n)
     # batched and served forms: single-GPU runs only (replicas would repeat them per rank)
+    if ws == 1 and not args.no_extras:
+        line["next_rows"] = run_extras(args, w)
     if ws == 1 and not args.no_mixed:
         w.close()
         line["mixed_precision"] = run_mixed(args, local)
@@ -516,6 +518,89 @@ def run_batched(args, local):
         "speedup": batched["world_steps_per_s"] / plain["world_steps_per_s"],
         "latency_note": "plain: one world's step alone; batched: one batched step (advances every world)",
     }
+
+
+def run_extras(args, w):
+    """The widened rows on the benchmark world (2048^2): the light block
+    (light_mode 1: one propagation round, and a full sweep, device time per
+    call), scene files (save and load of the whole world, wall time, through
+    the public API) and the asynchronous ledger (wall time from request to
+    availability, polling)."""
+    import ribo_world as rw
+
+    out = {}
+    saved_bytes = bytes(w.settings)
+    # light block: propagation rounds, then sweeps (a gamma upload marks the light dirty)
+    w.settings.light_mode = 1
+    w.settings.light_rows_per_step = 1
+    w.run(2)
+    w.sync()
+    k = 20
+    w.enable_kernel_timing(True)
+    kern = {}
+    for _ in range(k):
+        w.encode_steps(1)
+        for name, launches, kms, b in w.read_kernel_timing():
+            e = kern.setdefault(name, [0, 0.0, 0.0])
+            e[0] += launches
+            e[1] += kms
+            e[2] += b
+    w.enable_kernel_timing(False)
+    prop = kern.get("light_propagate", [1, 0.0, 0.0])
+    comm = kern.get("light_commit", [1, 0.0, 0.0])
+    w.settings.light_rows_per_step = 0
+    w.settings.light_interval = 1
+    w.enable_kernel_timing(True)
+    sweep = [0, 0.0, 0.0]
+    for _ in range(3):
+        w.encode_steps(1)
+        for name, launches, kms, b in w.read_kernel_timing():
+            if name in ("light_transmit", "uv_light"):
+                sweep[0] += 1 if name == "uv_light" else 0
+                sweep[1] += kms
+                sweep[2] += b
+    w.enable_kernel_timing(False)
+    out["light_block"] = {
+        "workload": "2048^2 world, light grid 1024^2 x 2 bands",
+        "propagate_round_ms": (prop[1] + comm[1]) / max(prop[0], 1),
+        "propagate_round_gbs": (prop[2] + comm[2]) / max(prop[1] + comm[1], 1e-9) / 1e6,
+        "full_sweep_ms": sweep[1] / max(sweep[0], 1),
+    }
+    import ctypes as _ct
+    _ct.memmove(_ct.byref(w.settings), saved_bytes, len(saved_bytes))
+    # scene files
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "bench.ribo")
+        w.sync()
+        t = time.perf_counter()
+        w.save_scene(path)
+        t_save = time.perf_counter() - t
+        size = os.path.getsize(path)
+        raw = sum(w.read(f).nbytes for f in (rw.CHEM, rw.GAMMA, rw.VELOCITY, rw.PRESSURE, rw.TEMP, rw.REDOX,
+                                              rw.HEAT, rw.LIGHT, rw.SHADE))
+        t = time.perf_counter()
+        w.load_scene(path)
+        t_load = time.perf_counter() - t
+    _ct.memmove(_ct.byref(w.settings), saved_bytes, len(saved_bytes))
+    out["scene_io"] = {"raw_mb": raw / 1e6, "file_mb": size / 1e6, "save_s": t_save, "load_s": t_load,
+                       "save_mb_per_s": raw / 1e6 / t_save, "load_mb_per_s": raw / 1e6 / t_load,
+                       "note": "host LZ4 block coding, single thread; includes the device copies"}
+    # asynchronous ledger
+    lat = []
+    for _ in range(20):
+        w.encode_steps(1)
+        t = time.perf_counter()
+        w.request_ledger()
+        got = None
+        while got is None:
+            got = w.poll_ledger()
+        lat.append((time.perf_counter() - t) * 1e3)
+    w.sync()
+    out["async_ledger"] = {"request_to_ready_ms_p50": percentile(lat, 50), "request_to_ready_ms_p99": percentile(lat, 99),
+                           "note": "requested right after one step was recorded: includes that step's device time"}
+    return out
 
 
 def run_mixed(args, local):
@@ -701,6 +786,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--mixed-steps", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
