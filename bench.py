@@ -600,6 +600,69 @@ def run_extras(args, w):
     w.sync()
     out["async_ledger"] = {"request_to_ready_ms_p50": percentile(lat, 50), "request_to_ready_ms_p99": percentile(lat, 99),
                            "note": "requested right after one step was recorded: includes that step's device time"}
+    out["terrain_block"] = run_terrain(args)
+    return out
+
+
+def run_terrain(args):
+    """The terrain grains (terrain_mode 1) on a world of the benchmark's size
+    with 10 % rubble next to the 10 % rock, reference defaults and grains
+    settling (sediment_settle 0.5: grain_fall on one step in four): the step
+    rate with the terrain block against the same world with the terrain
+    frozen, and the device time per step of each terrain kernel."""
+    import numpy as np
+    import ribo_world as rw
+    import synth
+
+    n = args.size
+    inputs = synth.make_world_inputs(n, seed=1001, rubble_frac=0.1)
+    w = rw.World(n, seed=1001, mg_min_size=16, mg_pre=3, mg_post=3)
+    w.seed_inputs(inputs)
+    w.params = synth.bench_params(1001)
+    w.params.sediment_settle = 0.5
+    w.settings.fluid_substep = 1
+    w.settings.mg_cycles = 4
+    rate = {}
+    k = 64
+    for mode in (1, 0, 1):
+        w.settings.terrain_mode = mode
+        w.run(8)
+        w.sync()
+        w.mark(0)
+        w.run(k)
+        w.mark(1)
+        rate[mode] = k / (w.elapsed_ms(0, 1) / 1000.0)
+    w.settings.terrain_mode = 1
+    w.enable_kernel_timing(True)
+    kern = {}
+    steps = 8
+    for _ in range(steps):
+        w.encode_steps(1)
+        for name, launches, kms, b in w.read_kernel_timing():
+            if name in ("relax_a", "relax_b", "relax_apply", "terrain_evict", "grain_fall", "compute_gamma_slope",
+                        "build_solid_mask", "wall_normals"):
+                e = kern.setdefault(name, [0, 0.0, 0.0])
+                e[0] += launches
+                e[1] += kms
+                e[2] += b
+    w.enable_kernel_timing(False)
+    gam = w.read(rw.GAMMA)
+    moved = int((gam != inputs[rw.GAMMA]).sum())
+    grains_ok = int(gam.sum(dtype=np.uint64)) == int(inputs[rw.GAMMA].sum(dtype=np.uint64))
+    seeded = rw.Ledger.from_cells(inputs[rw.CHEM])
+    led = w.ledger_blocking()
+    terrain_ms = sum(e[1] for e in kern.values()) / steps
+    out = {
+        "workload": f"{n}^2 world, 10% rock + 10% rubble (1-2 grains), reference defaults, sediment_settle 0.5",
+        "world_steps_per_s_terrain": rate[1],
+        "world_steps_per_s_frozen": rate[0],
+        "terrain_ms_per_step": terrain_ms,
+        "per_kernel_ms_per_step": {name: e[1] / steps for name, e in sorted(kern.items())},
+        "cells_changed": moved,
+        "grains_conserved": grains_ok,
+        "matter_conserved": [led.channel(c) for c in range(4)] == [seeded.channel(c) for c in range(4)],
+    }
+    del w
     return out
 
 

@@ -202,6 +202,11 @@ typedef struct ribo_world_settings {
   uint32_t light_rows_per_step;  // light_mode 1: rows the light propagates per step (at most 16); 0 = a full
                                  // sweep every light_interval steps [1]
   uint32_t light_interval;       // steps between full sweeps when light_rows_per_step = 0 [10]
+  // Terrain grains (shaders/world/terrain.wgsl:135-460, src/world/mod.rs:1497-1504):
+  uint32_t terrain_mode;  // 0 = GAMMA is a frozen input [default]; 1 = the reference's terrain block (two
+                          // relax passes, grain_fall when sediment_settle > 0, the slope) opens every step
+                          // and the wall mask is rebuilt at every fluid step.  Single worlds with the
+                          // f32 pressure solve only (batches and mixed precision reject it).
 } ribo_world_settings;
 
 // Device fields a caller can upload / read.  Sizes in bytes, for a world with
@@ -255,6 +260,15 @@ ribo_status ribo_world_get_settings(const ribo_world* w, ribo_world_settings* ou
 // copies `bytes` (must equal the field size) from host memory.  Uploading
 // GAMMA recomputes the slope and the fluid wall mask.
 ribo_status ribo_world_upload(ribo_world* w, ribo_field field, const void* host, size_t bytes);
+
+// World::encode_paint (src/world/mod.rs:1220-1241) with paint_terrain
+// (shaders/world/terrain.wgsl:385-413): `grains` (at most 6) grains in every
+// cell whose centre lies in the disc (centre and radius in cells), the
+// monomers that no longer fit evicted to a neighbour with room, in the
+// order of the terrain block (all stores, then the eviction loops by
+// 3 x 3 class of the cell).  The slope and wall mask are re-derived and the
+// next light block sweeps.
+ribo_status ribo_world_paint_terrain(ribo_world* w, float cx, float cy, float radius, uint32_t grains);
 
 // read_cells_blocking / read_f32_blocking (src/world/mod.rs:1801-1809):
 // waits for the world's stream, then copies the field to host memory.

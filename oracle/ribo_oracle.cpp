@@ -101,6 +101,17 @@ const float SUN_WATER_ABSORB = (float)0.05;
 const int LIGHT_TAPS = 7;
 const float SHADE_ONE = (float)100.0;
 const float MG_EPS = (float)1e-4;
+// terrain grains (shaders/world/terrain.wgsl:6-34, transport.wgsl:41)
+const uint32_t SANDPILE_DIFF = 3u;
+const float GAMMA_RELAX_P = (float)0.12;
+const float GAMMA_STRAY_WALK_P = (float)0.05;
+const float GAMMA_SEDIMENT_FACTOR = (float)0.5;
+const float GAMMA_SETTLE_SPEED = (float)0.5;
+const uint32_t GAMMA_ROCK_FULL = 6u;
+const float VENT_BLOW = (float)8.0;
+const float GAMMA_SHED_P = (float)0.03;
+const float GRAIN_ADV_CAP = (float)0.9;
+const size_t NO_CELL = ~(size_t)0;
 
 static inline uint32_t atomic_add_u32(uint32_t* p, uint32_t v) {
   return __atomic_fetch_add(p, v, __ATOMIC_RELAXED);
@@ -428,6 +439,322 @@ struct Oracle {
         float u = (float)cfg.world_units_per_cell;
         slope[(size_t)y * gw + x] = v2(dx / u, dy / u);
       }
+  }
+
+  // ---- terrain grains (shaders/world/terrain.wgsl:36-460) ----
+  //
+  // The reference runs these passes with in-place atomics: every cell's
+  // thread reads its neighbours' live grain counts while other threads move
+  // grains and evict monomers, so a GPU run has no single result.  The oracle
+  // executes ONE legal serialization of that program, the one the CUDA
+  // kernels reproduce exactly:
+  //  relax pass: every thread's decision reads (all grain counts read
+  //    before any move); then every take and add of a grain; then the
+  //    eviction loops of the moved grains' destinations, in nine classes
+  //    (x mod 3, y mod 3) of the destination, ascending destination index in
+  //    a class, the arrivals at one destination by ascending source index;
+  //  grain_fall: the columns in three classes (x mod 3), each column's loop
+  //    run whole, ascending x in a class;
+  //  paint: every store, then the eviction loops in the nine classes.
+  // Destinations of one class are >= 3 cells apart and an eviction loop only
+  // touches cells within one cell of its destination, so the order inside a
+  // class changes nothing: the GPU runs a class in parallel.
+
+  // transport.wgsl:54-58
+  float parcel_hop_p(V2 v) const {
+    const float env_per_fluid = (float)gw / (float)fw;
+    const float l1 = rb_abs(v.x) + rb_abs(v.y);
+    return rb_clamp(l1 * env_per_fluid * rb_max(P->dt, (float)1e-3), 0.0f, GRAIN_ADV_CAP);
+  }
+  // terrain.wgsl:24-28
+  V2 fluid_vel_at_cell(uint32_t cx, uint32_t cy) const {
+    uint32_t fx = std::min(cx * (uint32_t)fw / (uint32_t)gw, (uint32_t)fw - 1u);
+    uint32_t fy = std::min(cy * (uint32_t)fh / (uint32_t)gh, (uint32_t)fh - 1u);
+    return sanitize(vel_a[fgrid(fx, fy)]);
+  }
+  // terrain.wgsl:54-72
+  size_t evict_target(size_t src, size_t dst) const {
+    if (chem_cell_total(src) < chem_capacity(src)) return src;
+    const int x = (int)(dst % gw), y = (int)(dst / gw);
+    const int nx[4] = {x + 1, x - 1, x, x}, ny[4] = {y, y, y + 1, y - 1};
+    size_t not_rock = gamma_count(src) < GAMMA_SOLID ? src : NO_CELL;
+    for (int k = 0; k < 4; k++) {
+      if (nx[k] < 0 || ny[k] < 0 || nx[k] >= gw || ny[k] >= gh) continue;
+      size_t n = (size_t)ny[k] * gw + nx[k];
+      if (chem_cell_total(n) < chem_capacity(n)) return n;
+      if (not_rock == NO_CELL && gamma_count(n) < GAMMA_SOLID) not_rock = n;
+    }
+    return not_rock == NO_CELL ? src : not_rock;
+  }
+  // The eviction loop of gamma_move_one (terrain.wgsl:82-100) and of
+  // paint_terrain (:396-412, src == dst): one monomer per round, the spent
+  // state of a channel before its activated state, channels in order.
+  void evict(size_t src, size_t dst) {
+    const uint32_t cap = chem_capacity(dst);
+    for (int guard = 0; guard < 64; guard++) {
+      if (chem_cell_total(dst) <= cap) break;
+      const size_t to = evict_target(src, dst);
+      if (to == dst) break;
+      bool moved = false;
+      for (int c = 0; c < 4 && !moved; c++) {
+        uint32_t& v = chem[dst * 4 + c];
+        if ((v >> 16) != 0u) {
+          v -= CHEM_SPENT_ONE;
+          chem[to * 4 + c] += CHEM_SPENT_ONE;
+          moved = true;
+        } else if ((v & CHEM_STATE_MASK) != 0u) {
+          v -= 1u;
+          chem[to * 4 + c] += 1u;
+          moved = true;
+        }
+      }
+      if (!moved) break;
+    }
+  }
+  // terrain.wgsl:137-159
+  bool compaction_stable(size_t src, size_t dst, uint32_t n, uint32_t c) const {
+    const int dx4[4] = {1, -1, 0, 0}, dy4[4] = {0, 0, 1, -1};
+    const int xd = (int)(dst % gw), yd = (int)(dst / gw), xs = (int)(src % gw), ys = (int)(src / gw);
+    bool ok = true;
+    for (int k = 0; k < 4; k++) {
+      int qx = xd + dx4[k], qy = yd + dy4[k];
+      if (qx >= 0 && qy >= 0 && qx < gw && qy < gh) {
+        size_t qi = (size_t)qy * gw + qx;
+        uint32_t low = qi == src ? n - 1u : gamma_count(qi);
+        if (c + 1u >= low + SANDPILE_DIFF) ok = false;
+      }
+      qx = xs + dx4[k];
+      qy = ys + dy4[k];
+      if (qx >= 0 && qy >= 0 && qx < gw && qy < gh) {
+        size_t qi = (size_t)qy * gw + qx;
+        uint32_t high = qi == dst ? c + 1u : gamma_count(qi);
+        if (high >= n - 1u + SANDPILE_DIFF) ok = false;
+      }
+    }
+    return ok;
+  }
+  // terrain.wgsl:161-372 (relax_gamma_pass), the decision of one cell from
+  // the grain counts as they are: the destination of its grain, or idx.
+  size_t relax_decide(size_t idx, uint32_t phase) const {
+    const int x = (int)(idx % gw), y = (int)(idx / gw);
+    const uint32_t n = gamma_count(idx);
+    if (n == 0u) return idx;
+    if (n < SANDPILE_DIFF) {
+      // loose grains
+      uint32_t bonds = 0u, best_c = 0xFFFFu, comp_c = 0u;
+      int best_score = -1, em_score = -1;
+      size_t best = idx, em = idx, comp = idx;
+      bool em_found = false;
+      const rb_u4 rr = rb_pcg4d((uint32_t)idx, P->epoch, RB_S_RELAX + phase, P->seed);
+      uint32_t tie = rr.x;
+      const float comp_roll = (float)(rb_hash32(rr.x ^ 0x5bd1e995u) >> 8) * (1.0f / 16777216.0f);
+      const bool try_comp = comp_roll < P->sediment_compaction;
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          if (dx == 0 && dy == 0) continue;
+          const int nx = x + dx, ny = y + dy;
+          if (nx < 0 || ny < 0 || nx >= gw || ny >= gh) continue;
+          const size_t ni = (size_t)ny * gw + nx;
+          const uint32_t c = gamma_count(ni);
+          if (c >= 1u) bonds++;
+          if (try_comp && c >= 1u && c < GAMMA_ROCK_FULL &&
+              (c > comp_c || (c == comp_c && (rb_hash32(tie ^ ((uint32_t)ni * 31u)) & 1u) == 1u)) &&
+              compaction_stable(idx, ni, n, c)) {
+            comp_c = c;
+            comp = ni;
+          }
+          if (c <= n) {
+            int score = 0;
+            for (int sy = -1; sy <= 1; sy++)
+              for (int sx = -1; sx <= 1; sx++) {
+                if (sx == 0 && sy == 0) continue;
+                const int qx = nx + sx, qy = ny + sy;
+                if (qx < 0 || qy < 0 || qx >= gw || qy >= gh) continue;
+                const size_t qi = (size_t)qy * gw + qx;
+                if (qi == idx) continue;
+                if (gamma_count(qi) >= 1u) score++;
+              }
+            tie = rb_hash32(tie ^ (uint32_t)ni);
+            if (score > best_score || (score == best_score && c < best_c) ||
+                (score == best_score && c == best_c && (tie & 1u) == 1u)) {
+              best_score = score;
+              best_c = c;
+              best = ni;
+            }
+            if (c == 0u && (score > em_score || (score == em_score && (tie & 2u) == 2u))) {
+              em_score = score;
+              em = ni;
+              em_found = true;
+            }
+          }
+        }
+      // pow(0.25, bonds): 2^(-2 bonds) is exact in f32 for bonds <= 8
+      const float mob = ldexpf(1.0f, -2 * (int)bonds);
+      if (try_comp && bonds >= 3u && comp != idx &&
+          comp_roll < P->sediment_compaction * (float)(bonds - 2u) / 6.0f)
+        return comp;
+      V2 vs = v2(0.0f, 0.0f);
+      if (P->fluid_enabled != 0u) {
+        const int dx4[4] = {1, -1, 0, 0}, dy4[4] = {0, 0, 1, -1};
+        for (int k = 0; k < 4; k++) {
+          const int qx = x + dx4[k], qy = y + dy4[k];
+          if (qx < 0 || qy < 0 || qx >= gw || qy >= gh) continue;
+          if (gamma_count((size_t)qy * gw + qx) != 0u) continue;
+          const V2 v = fluid_vel_at_cell((uint32_t)qx, (uint32_t)qy);
+          if (dot(v, v) > dot(vs, vs)) vs = v;
+        }
+      }
+      const bool unsupported = y > 0 && gamma_count(idx - gw) == 0u;
+      V2 v_move = v2(0.0f, 0.0f);
+      float p_sed = 0.0f;
+      if (unsupported && bonds == 0u) {
+        v_move = vs;
+        p_sed = parcel_hop_p(v_move);
+      } else {
+        const float speed = length(vs);
+        const float crit = rb_max(P->sediment_threshold, 0.0f) * (1.0f + rb_max(P->sediment_cohesion, 0.0f) * (float)bonds);
+        const float excess = rb_max(speed - crit, 0.0f);
+        v_move = speed > (float)1e-6 ? vs * (excess / rb_max(speed, (float)1e-6)) : v2(0.0f, 0.0f);
+        p_sed = parcel_hop_p(v_move) * GAMMA_SEDIMENT_FACTOR * rb_max(P->sediment_transport, 0.0f);
+      }
+      const uint32_t hfx = std::min((uint32_t)x * (uint32_t)fw / (uint32_t)gw, (uint32_t)fw - 1u);
+      const uint32_t hfy = std::min((uint32_t)y * (uint32_t)fh / (uint32_t)gh, (uint32_t)fh - 1u);
+      const V2 vent = heat[fgrid(hfx, hfy)];
+      const float blow = VENT_BLOW * rb_max(vent.x, vent.y);
+      if (blow > 0.0f) {
+        v_move = v2((rr.y & 1u) == 1u ? (float)0.6 : (float)-0.6, 1.0f) * blow;
+        p_sed = rb_max(p_sed, parcel_hop_p(v_move));
+      }
+      if (bonds >= 4u && p_sed <= 0.0f) return idx;
+      const uint32_t hw = rr.y;
+      const float rw = rb_u2f(rr.z), rw2 = rb_u2f(rr.w);
+      if (n >= 2u && em_found && rw2 < GAMMA_SHED_P * rb_clamp(P->sediment_settle, 0.0f, 1.0f)) return em;
+      if (rw < p_sed) {
+        int ddx = 0, ddy = 0;
+        const float ax = rb_abs(v_move.x), ay = rb_abs(v_move.y);
+        if (rb_u2f(hw) < ax / rb_max(ax + ay, (float)1e-6))
+          ddx = v_move.x > 0.0f ? 1 : -1;
+        else
+          ddy = v_move.y > 0.0f ? 1 : -1;
+        const int wx = x + ddx, wy = y + ddy;
+        if (wx >= 0 && wy >= 0 && wx < gw && wy < gh) {
+          const size_t wi = (size_t)wy * gw + wx;
+          if (gamma_count(wi) <= n) return wi;
+        }
+        return idx;
+      }
+      if (rw < p_sed + GAMMA_STRAY_WALK_P * mob) {
+        if (best_score > (int)bonds) return best;
+        if (bonds == 0u) {
+          static const int wdx[8] = {1, -1, 0, 0, 1, -1, 1, -1}, wdy[8] = {0, 0, 1, -1, 1, 1, -1, -1};
+          const uint32_t k = (hw >> 8) % 8u;
+          const int wx = x + wdx[k], wy = y + wdy[k];
+          if (wx >= 0 && wy >= 0 && wx < gw && wy < gh) {
+            const size_t wi = (size_t)wy * gw + wx;
+            if (gamma_count(wi) <= n) return wi;
+          }
+        }
+      }
+      return idx;
+    }
+    // sandpile: slide towards the lowest of the four neighbours
+    size_t best = idx;
+    uint32_t best_c = n;
+    if (x > 0 && gamma_count(idx - 1) < best_c) { best_c = gamma_count(idx - 1); best = idx - 1; }
+    if (x + 1 < gw && gamma_count(idx + 1) < best_c) { best_c = gamma_count(idx + 1); best = idx + 1; }
+    if (y > 0 && gamma_count(idx - gw) < best_c) { best_c = gamma_count(idx - gw); best = idx - gw; }
+    if (y + 1 < gh && gamma_count(idx + gw) < best_c) { best_c = gamma_count(idx + gw); best = idx + gw; }
+    if (best == idx || n - best_c < SANDPILE_DIFF) return idx;
+    const float p = GAMMA_RELAX_P * rb_max(rb_clamp(P->sediment_settle, 0.0f, 1.0f), rb_clamp(P->rock_crumble, 0.0f, 1.0f));
+    if (rb_u2f(rb_pcg4d((uint32_t)idx, P->epoch, RB_S_SAND + phase, P->seed).x) < p) return best;
+    return idx;
+  }
+  static int cell_class(int x, int y) { return x % 3 + 3 * (y % 3); }
+  // relax_gamma_a / relax_gamma_b (terrain.wgsl:449-459) in the order above
+  void relax_pass(uint32_t phase) {
+    const size_t C = cells();
+    std::vector<size_t> dest(C);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)C; i++) dest[i] = relax_decide((size_t)i, phase);
+    std::vector<uint8_t> arrived(C, 0);
+    for (size_t i = 0; i < C; i++)
+      if (dest[i] != i) {
+        gamma[i] -= 1u;
+        gamma[dest[i]] += 1u;
+        arrived[dest[i]] = 1;
+      }
+    for (int cls = 0; cls < 9; cls++)
+      for (int y = cls / 3; y < gh; y += 3)
+        for (int x = cls % 3; x < gw; x += 3) {
+          const size_t dst = (size_t)y * gw + x;
+          if (!arrived[dst]) continue;
+          for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+              const int sx = x + dx, sy = y + dy;
+              if ((dx == 0 && dy == 0) || sx < 0 || sy < 0 || sx >= gw || sy >= gh) continue;
+              const size_t src = (size_t)sy * gw + sx;
+              if (dest[src] == dst) evict(src, dst);
+            }
+        }
+  }
+  // terrain.wgsl:425-446 (grain_fall)
+  void grain_fall() {
+    const float w_s = GAMMA_SETTLE_SPEED * rb_max(P->sediment_settle, 0.0f);
+    const float rate = parcel_hop_p(v2(0.0f, w_s));
+    if (rate <= 0.0f) return;
+    const uint32_t rf = rb_f2u(rate * 65536.0f);
+    if (((P->epoch * rf) >> 16) == (((P->epoch + 1u) * rf) >> 16)) return;
+    for (int cls = 0; cls < 3; cls++)
+      for (int x = cls; x < gw; x += 3) {
+        bool supported = true;
+        for (int y = 0; y < gh; y++) {
+          const size_t idx = (size_t)y * gw + x;
+          const uint32_t n = gamma_count(idx);
+          if (n == 0u) {
+            supported = false;
+            continue;
+          }
+          if (n >= GAMMA_SOLID) {
+            supported = true;
+            continue;
+          }
+          if (supported) continue;
+          for (uint32_t k = 0; k < n; k++) {
+            gamma[idx] -= 1u;
+            gamma[idx - gw] += 1u;
+            evict(idx, idx - gw);
+          }
+        }
+      }
+  }
+  // World::encode_paint (src/world/mod.rs:1220-1241), paint_terrain (terrain.wgsl:390-413)
+  void paint(float cx, float cy, float radius, uint32_t grains) {
+    const uint32_t want = std::min(grains, 6u);
+    std::vector<uint8_t> painted(cells(), 0);
+    for (int y = 0; y < gh; y++)
+      for (int x = 0; x < gw; x++) {
+        const float ex = (float)x + 0.5f - cx, ey = (float)y + 0.5f - cy;
+        if (ex * ex + ey * ey > radius * radius) continue;
+        gamma[(size_t)y * gw + x] = want;
+        painted[(size_t)y * gw + x] = 1;
+      }
+    for (int cls = 0; cls < 9; cls++)
+      for (int y = cls / 3; y < gh; y += 3)
+        for (int x = cls % 3; x < gw; x += 3) {
+          const size_t i = (size_t)y * gw + x;
+          if (painted[i]) evict(i, i);
+        }
+    compute_slope();
+    build_solid_mask();
+    light_dirty = true;
+  }
+  // src/world/mod.rs:1497-1504: relax a, relax b, grain_fall when grains
+  // settle, then the slope
+  void terrain_block() {
+    relax_pass(0u);
+    relax_pass(1u);
+    if (P->sediment_settle > 0.0f) grain_fall();
+    compute_slope();
   }
 
   // fluid.wgsl:185-189
@@ -1213,6 +1540,7 @@ struct Oracle {
     P = p;
     uint32_t epoch = p->epoch;
     uint32_t substep = std::min(std::max(st.fluid_substep, 1u), 4u);
+    if (st.terrain_mode) terrain_block();
     if (st.light_mode) light_block(epoch);
     if (st.fluid_enabled && epoch % substep == 0u) {
       build_solid_mask();
@@ -1393,7 +1721,8 @@ int orc_get_threads(void) {
 // 0 mask, 1 temperature(+copy), 2 forces(buoyancy, gather, clear), 3 add_forces a->b,
 // 4 diffuse b->a, 5 advect a->b, 6 vorticity b->a, 7 divergence(a), 8 pressure solve,
 // 9 subtract_gradient a->b, 10 net_flux(b), 11 boundaries b->a, 12 smooth(a),
-// 13 thermal, 14 agg_count+agg_neighbours, 15 transport scatter+commit.
+// 13 thermal, 14 agg_count+agg_neighbours, 15 transport scatter+commit,
+// 16 relax pass a, 17 relax pass b, 18 grain_fall.
 void orc_pass(void* w, const ribo_sim_params* p, int which) {
   Oracle* o = (Oracle*)w;
   o->P = p;
@@ -1414,7 +1743,16 @@ void orc_pass(void* w, const ribo_sim_params* p, int which) {
     case 13: o->thermal_activation(); break;
     case 14: o->agg_count(); o->agg_neighbours(); break;
     case 15: o->transport_scatter(); o->transport_commit(); break;
+    case 16: o->relax_pass(0u); break;
+    case 17: o->relax_pass(1u); break;
+    case 18: o->grain_fall(); break;
   }
+}
+
+// World::encode_paint: `grains` grains in every cell of the disc (centre and
+// radius in cells), the monomers that no longer fit evicted.
+void orc_paint(void* w, float cx, float cy, float radius, uint32_t grains) {
+  ((Oracle*)w)->paint(cx, cy, radius, grains);
 }
 
 // Reads velocity_b (the intermediate velocity buffer) for per-pass tests.

@@ -42,6 +42,7 @@ def load():
             "orc_set_threads": ([ctypes.c_int], None),
             "orc_get_threads": ([], ctypes.c_int),
             "orc_pass": ([vp, P(rw.SimParams), ctypes.c_int], None),
+            "orc_paint": ([vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_uint32], None),
             "orc_read_vel_b": ([vp, vp, ctypes.c_size_t], ctypes.c_int),
             "orc_write_vel_b": ([vp, vp, ctypes.c_size_t], ctypes.c_int),
             "orc_exp": ([ctypes.c_float], ctypes.c_float),
@@ -192,6 +193,9 @@ class OracleWorld:
     def run_pass(self, params: "rw.SimParams", which: int):
         self._lib.orc_set_settings(self._h, ctypes.byref(self.settings))
         self._lib.orc_pass(self._h, ctypes.byref(params), which)
+
+    def encode_paint(self, cx: float, cy: float, radius: float, grains: int):
+        self._lib.orc_paint(self._h, cx, cy, radius, grains)
 
     def ledger_blocking(self) -> "rw.Ledger":
         out = (ctypes.c_uint32 * 12)()

@@ -498,6 +498,9 @@ ribo_status Batch::step(const ribo_sim_params* per_step, uint32_t n, const uint3
   for (size_t k = 0; k < worlds.size(); k++)
     if (worlds[k]->st.light_mode)
       return set_error(RIBO_INVALID_ARG, "member %zu: batches take worlds whose light is a frozen input (light_mode 0)", k);
+  for (size_t k = 0; k < worlds.size(); k++)
+    if (worlds[k]->st.terrain_mode)
+      return set_error(RIBO_INVALID_ARG, "member %zu: batches take worlds whose terrain is a frozen input (terrain_mode 0)", k);
   RB_TRY(bind(), "device");
   {
     ribo_status s = ensure_capacity();

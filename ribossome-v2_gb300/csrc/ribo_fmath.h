@@ -268,5 +268,20 @@ RB_HD float rb_u2f(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0f); 
 #define RB_S_DECAY 2u
 #define RB_S_THERMAL 3u
 #define RB_S_BUOYANCY 4u
+#define RB_S_RELAX 16u  // + relax phase (0, 1)
+#define RB_S_SAND 32u   // + relax phase (0, 1)
 #define RB_S_MOVE (1u << 16)
 #define RB_S_DISPERSE (6u << 16)
+
+// Integer mixer of tie-breaks (not a random stream): shift-xor-multiply with
+// the "lowbias32" constants of C. Wellons' hash-prospector, as the
+// reference's hash() (shaders/common/rng.wgsl:46-50).
+RB_HD uint32_t rb_hash32(uint32_t v) {
+  uint32_t x = v;
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}

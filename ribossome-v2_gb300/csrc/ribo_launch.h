@@ -81,6 +81,22 @@ void launch_light_sweep(const Dev& d, const ribo_sim_params* P, cudaStream_t s);
 void launch_light_propagate(const Target& t, cudaStream_t s);
 void launch_light_commit(const Target& t, cudaStream_t s);
 
+// terrain.cu (terrain_mode 1, and the terrain brush)
+struct TerrainBufs {
+  uint32_t* gamma;  // grains per cell, updated in place
+  uint8_t* code;    // per cell: 0 = its grain stays; 1 + k = it moves to the k-th of its 8 neighbours
+                    // in ascending cell index (centre skipped)
+  uint32_t* list;   // cells that received a grain (relax) or were painted, each at most once
+  uint32_t* count;  // entries in list (the eviction kernel empties it)
+};
+// One relax pass (relax_gamma_a for phase 0, _b for phase 1): decisions,
+// moves, eviction loops.
+void launch_relax(const Dev& d, const ribo_sim_params* P, const TerrainBufs& t, uint32_t phase, cudaStream_t s);
+// grain_fall: three launches (columns x mod 3); each returns at once on steps
+// the fall clock does not tick.
+void launch_grain_fall(const Dev& d, const ribo_sim_params* P, const TerrainBufs& t, cudaStream_t s);
+void launch_paint(const Dev& d, const TerrainBufs& t, float cx, float cy, float radius, uint32_t grains, cudaStream_t s);
+
 // fluid.cu
 void launch_solid_mask(const Target& t, cudaStream_t s);
 void launch_temperature(const Target& t, cudaStream_t s);

@@ -79,6 +79,11 @@ struct World {
   uint32_t* shade = nullptr;
   float2* slope = nullptr;
   uint32_t *agg_act = nullptr, *agg_nb = nullptr;
+  // terrain grains (terrain_mode 1 and the brush)
+  uint8_t* terrain_code = nullptr;
+  uint32_t* terrain_list = nullptr;
+  uint32_t* terrain_count = nullptr;
+  TerrainBufs terrain_bufs() const { return TerrainBufs{gamma, terrain_code, terrain_list, terrain_count}; }
   // fluid resolution
   uint8_t* mask = nullptr;
   float2* normal = nullptr;
@@ -130,6 +135,10 @@ struct World {
   ribo_status init(const ribo_world_cfg& c);
   ~World();
   ribo_status upload(ribo_field f, const void* host, size_t bytes);
+  ribo_status paint_terrain(float cx, float cy, float radius, uint32_t grains);
+  // re-derives what the world keeps from gamma (slope, wall mask, the mixed
+  // solver's setup) after gamma changed outside a step
+  ribo_status terrain_changed();
   ribo_status read(ribo_field f, void* host, size_t bytes);
   ribo_status step(const ribo_sim_params* per_step, uint32_t n);
   ribo_status ledger_read(uint32_t out[12]);

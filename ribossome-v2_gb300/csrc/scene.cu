@@ -598,7 +598,7 @@ const SettingField SETTINGS[] = {RB_SETTING(fluid_enabled),  RB_SETTING(fluid_su
                                  RB_SETTING(mg_unfused),     RB_SETTING(transport_simple), RB_SETTING(mixed_tol),
                                  RB_SETTING(mixed_inner_tol), RB_SETTING(mixed_max_outer), RB_SETTING(mixed_max_inner),
                                  RB_SETTING(mixed_alpha),    RB_SETTING(light_mode),      RB_SETTING(light_rows_per_step),
-                                 RB_SETTING(light_interval)};
+                                 RB_SETTING(light_interval), RB_SETTING(terrain_mode)};
 #undef RB_SETTING
 static_assert(sizeof(SETTINGS) / sizeof(SETTINGS[0]) * 4 == sizeof(ribo_world_settings), "every setting is named");
 

@@ -247,6 +247,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   const size_t M = build_levels((int)c.fluid_w, (int)c.fluid_h, c.mg_min_size ? c.mg_min_size : 8, lv);
   size_t b = 0;
   b += C * (16 + 16 + 4 + 8 + 4 + 4);                             // chem a/b, gamma, slope, agg_act, agg_nb
+  b += C * (1 + 4) + 16;                                          // terrain move codes, eviction list, count
   b += 2 * L * 4 * 3;                                             // light, light_next, shade
   b += F * (1 + 8 + 4 + 8 * 3 + 4 * 3 + 4 * 5 + 8 * 3 + 4 + 4);  // mask..heat, mask32, p_tmp
   b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 * 2 + MAX_STEPS * 12 * 4 + 16;
@@ -285,6 +286,9 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(slope, C * 8);
   RB_ALLOC(agg_act, C * 4);
   RB_ALLOC(agg_nb, C * 4);
+  RB_ALLOC(terrain_code, C);
+  RB_ALLOC(terrain_list, C * 4);
+  RB_ALLOC(terrain_count, 16);
   RB_ALLOC(mask, F);
   RB_ALLOC(normal, F * 8);
   RB_ALLOC(curl, F * 4);
@@ -376,16 +380,33 @@ ribo_status World::upload(ribo_field f, const void* host, size_t bytes) {
     return set_error(RIBO_INVALID_ARG, "field %d is derived and read-only", (int)f);
   RB_TRY(cudaMemcpyAsync(field_ptr(f), host, bytes, cudaMemcpyHostToDevice, stream), "upload");
   if (f == RIBO_FIELD_GAMMA) {
-    Dev d = dev();
-    launch_slope(d, (float)cfg.world_units_per_cell, stream);
-    launch_solid_mask(target_one(d, nullptr), stream);
-    RB_TRY(cudaGetLastError(), "slope/mask");
-    ribo_status ms = mixed_setup(*this);
-    if (ms != RIBO_OK) return ms;
-    light_dirty = true;  // the terrain changed: the next light block sweeps
+    ribo_status r = terrain_changed();
+    if (r != RIBO_OK) return r;
   }
   RB_TRY(cudaStreamSynchronize(stream), "upload");
   return RIBO_OK;
+}
+
+ribo_status World::terrain_changed() {
+  Dev d = dev();
+  launch_slope(d, (float)cfg.world_units_per_cell, stream);
+  launch_solid_mask(target_one(d, nullptr), stream);
+  RB_TRY(cudaGetLastError(), "slope/mask");
+  ribo_status ms = mixed_setup(*this);
+  if (ms != RIBO_OK) return ms;
+  light_dirty = true;  // the terrain changed: the next light block sweeps
+  return RIBO_OK;
+}
+
+// World::encode_paint (src/world/mod.rs:1220-1241).
+ribo_status World::paint_terrain(float cx, float cy, float radius, uint32_t grains) {
+  RB_TRY(bind(), "device");
+  launch_paint(dev(), terrain_bufs(), cx, cy, radius, grains, stream);
+  RB_TRY(cudaGetLastError(), "paint");
+  ribo_status r = terrain_changed();
+  if (r != RIBO_OK) return r;
+  RB_TRY(cudaStreamSynchronize(stream), "paint");
+  return check_status();
 }
 
 namespace {
@@ -445,8 +466,17 @@ bool World::light_sweeps(const ribo_sim_params& hp, bool dirty) const {
   return dirty || (st.light_rows_per_step == 0 && hp.epoch % interval == 0u);
 }
 
-// The light, fluid and transport blocks of one step (src/world/mod.rs:1505-1601).
+// The terrain, light, fluid and transport blocks of one step
+// (src/world/mod.rs:1497-1601).
 void World::record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uint32_t i) {
+  if (st.terrain_mode) {
+    const Dev d = dev();
+    const TerrainBufs tb = terrain_bufs();
+    launch_relax(d, P, tb, 0u, stream);
+    launch_relax(d, P, tb, 1u, stream);
+    if (hp.sediment_settle > 0.0f) launch_grain_fall(d, P, tb, stream);
+    launch_slope(d, (float)cfg.world_units_per_cell, stream);
+  }
   if (st.light_mode) {
     const Target t = target_one(dev(), P);
     if (light_sweeps(hp, light_dirty)) {
@@ -463,6 +493,7 @@ void World::record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uin
   }
   uint32_t substep = st.fluid_substep < 1 ? 1 : (st.fluid_substep > 4 ? 4 : st.fluid_substep);
   if (st.fluid_enabled && hp.epoch % substep == 0u) {
+    if (st.terrain_mode) launch_solid_mask(target_one(dev(), P), stream);  // build_solid_mask
     launch_temperature(target_one(dev(), P), stream);  // temp_in -> temp_out
     std::swap(temp_cur, temp_nxt);                     // copy_temperature
     std::swap(redox_cur, redox_nxt);
@@ -499,6 +530,9 @@ ribo_status World::step(const ribo_sim_params* per_step, uint32_t n) {
   if (n == 0) return RIBO_OK;
   if (!per_step) return set_error(RIBO_INVALID_ARG, "null params");
   if (n > MAX_STEPS) return set_error(RIBO_INVALID_ARG, "%u steps per call (at most %u)", n, MAX_STEPS);
+  if (st.terrain_mode && mixed)
+    return set_error(RIBO_INVALID_ARG, "mixed precision takes a frozen terrain (terrain_mode 0): its solver setup "
+                                       "follows the wall mask of the uploaded gamma");
   RB_TRY(bind(), "device");
   // src/world/mod.rs:1414-1421: turning the fluid off clears it once.
   if (!st.fluid_enabled && fluid_was_on) {
@@ -559,7 +593,8 @@ std::string World::graph_key(const ribo_sim_params* per_step, uint32_t n, int sl
     const bool sweep = st.light_mode && light_sweeps(p, dirty);
     if (sweep) dirty = false;
     char c = (char)((st.fluid_enabled && p.epoch % substep == 0u ? 1 : 0) | (p.epoch % te == 0u ? 2 : 0) |
-                    (p.aggregation > 0.0f ? 4 : 0) | (sweep ? 8 : 0));
+                    (p.aggregation > 0.0f ? 4 : 0) | (sweep ? 8 : 0) |
+                    (st.terrain_mode && p.sediment_settle > 0.0f ? 16 : 0));
     k.push_back(c);
   }
   return k;
@@ -842,6 +877,11 @@ ribo_status ribo_world_get_settings(const ribo_world* w, ribo_world_settings* ou
 ribo_status ribo_world_upload(ribo_world* w, ribo_field field, const void* host, size_t bytes) {
   if (!w) return set_error(RIBO_INVALID_ARG, "null world");
   return w->w.upload(field, host, bytes);
+}
+
+ribo_status ribo_world_paint_terrain(ribo_world* w, float cx, float cy, float radius, uint32_t grains) {
+  if (!w) return set_error(RIBO_INVALID_ARG, "null world");
+  return w->w.paint_terrain(cx, cy, radius, grains);
 }
 
 ribo_status ribo_world_read(ribo_world* w, ribo_field field, void* host, size_t bytes) {

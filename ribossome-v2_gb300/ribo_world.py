@@ -72,6 +72,7 @@ class WorldSettings(ctypes.Structure):
         ("mixed_tol", ctypes.c_float), ("mixed_inner_tol", ctypes.c_float),
         ("mixed_max_outer", ctypes.c_uint32), ("mixed_max_inner", ctypes.c_uint32), ("mixed_alpha", ctypes.c_float),
         ("light_mode", ctypes.c_uint32), ("light_rows_per_step", ctypes.c_uint32), ("light_interval", ctypes.c_uint32),
+        ("terrain_mode", ctypes.c_uint32),
     ]
 
 
@@ -103,7 +104,7 @@ class ServerStats(ctypes.Structure):
                 ("world_steps", ctypes.c_uint64), ("iterations", ctypes.c_uint64), ("gpu_ms", ctypes.c_double)]
 
 
-assert ctypes.sizeof(WorldSettings) == 64 and ctypes.sizeof(Job) == 880 and ctypes.sizeof(JobResult) == 104
+assert ctypes.sizeof(WorldSettings) == 68 and ctypes.sizeof(Job) == 888 and ctypes.sizeof(JobResult) == 104
 assert ctypes.sizeof(ServerCfg) == 40
 
 
@@ -133,6 +134,7 @@ def load_library(path: str = LIB_PATH):
         "ribo_world_set_settings": ([vp, P(WorldSettings)], ctypes.c_int),
         "ribo_world_get_settings": ([vp, P(WorldSettings)], ctypes.c_int),
         "ribo_world_upload": ([vp, ctypes.c_int, vp, ctypes.c_size_t], ctypes.c_int),
+        "ribo_world_paint_terrain": ([vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_uint32], ctypes.c_int),
         "ribo_world_read": ([vp, ctypes.c_int, vp, ctypes.c_size_t], ctypes.c_int),
         "ribo_world_device_ptr": ([vp, ctypes.c_int, P(vp), P(ctypes.c_size_t)], ctypes.c_int),
         "ribo_world_step": ([vp, P(SimParams), ctypes.c_uint32], ctypes.c_int),
@@ -347,6 +349,12 @@ class World:
         shape, dt = self.field_shape(field)
         a = np.ascontiguousarray(array, dtype=dt).reshape(shape)
         check(self._lib.ribo_world_upload(self._h, field, a.ctypes.data, a.nbytes), f"upload {field}")
+
+    def encode_paint(self, cx: float, cy: float, radius: float, grains: int):
+        """World::encode_paint (src/world/mod.rs:1220-1241): `grains` (at most 6)
+        grains in every cell of the disc (centre and radius in cells); the
+        monomers that no longer fit are evicted to a neighbour with room."""
+        check(self._lib.ribo_world_paint_terrain(self._h, cx, cy, radius, grains), "paint")
 
     def read(self, field: int) -> np.ndarray:
         shape, dt = self.field_shape(field)

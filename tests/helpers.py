@@ -9,6 +9,7 @@ STATE_FIELDS = [
     (rw.REDOX, "redox"), (rw.DIVERGENCE, "divergence"), (rw.VEL_SMOOTH, "velocity_smooth"),
     (rw.NET_FLUX, "net_flux"), (rw.SOLID_MASK, "solid_mask"), (rw.SLOPE, "slope"),
     (rw.FORCE_VECTORS, "force_vectors"), (rw.REDOX_EATEN, "redox_eaten"), (rw.LIGHT, "light"),
+    (rw.GAMMA, "gamma"),
 ]
 
 

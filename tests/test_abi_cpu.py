@@ -127,7 +127,7 @@ def test_world_footprint_counts_every_buffer(rw):
                 nx, ny = nx // 2, ny // 2
             else:
                 break
-        want = C * 52 + 24 * L + F * 101 + (fw + fh) * 4 + 96 + 64 * 48 + 16 + M * 13 + 2 * 64 * 464
+        want = C * 57 + 24 * L + F * 101 + (fw + fh) * 4 + 96 + 64 * 48 + 32 + M * 13 + 2 * 64 * 464
         assert rw.world_footprint((gw, gh), (fw, fh), mg_min_size=mg) == want
 
 
