@@ -86,9 +86,12 @@ struct TerrainBufs {
   uint32_t* gamma;  // grains per cell, updated in place
   uint8_t* code;    // per cell: 0 = its grain stays; 1 + k = it moves to the k-th of its 8 neighbours
                     // in ascending cell index (centre skipped)
-  uint32_t* list;   // cells that received a grain (relax) or were painted, each at most once
-  uint32_t* count;  // entries in list (the eviction kernel empties it)
+  uint8_t* arrivals;  // per cell that received grains: bit k = the grain of its k-th neighbour arrived
+  uint32_t* list;   // cells that received a grain (relax) or were painted, each at most once, in nine
+                    // segments by class (x mod 3 + 3 (y mod 3)) of terrain_list_entries / 9 entries
+  uint32_t* count;  // [9] entries per segment (the eviction kernel empties them)
 };
+size_t terrain_list_entries(int gw, int gh);
 // One relax pass (relax_gamma_a for phase 0, _b for phase 1): decisions,
 // moves, eviction loops.
 void launch_relax(const Dev& d, const ribo_sim_params* P, const TerrainBufs& t, uint32_t phase, cudaStream_t s);

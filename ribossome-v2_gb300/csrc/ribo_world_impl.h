@@ -81,9 +81,12 @@ struct World {
   uint32_t *agg_act = nullptr, *agg_nb = nullptr;
   // terrain grains (terrain_mode 1 and the brush)
   uint8_t* terrain_code = nullptr;
+  uint8_t* terrain_arrivals = nullptr;
   uint32_t* terrain_list = nullptr;
   uint32_t* terrain_count = nullptr;
-  TerrainBufs terrain_bufs() const { return TerrainBufs{gamma, terrain_code, terrain_list, terrain_count}; }
+  TerrainBufs terrain_bufs() const {
+    return TerrainBufs{gamma, terrain_code, terrain_arrivals, terrain_list, terrain_count};
+  }
   // fluid resolution
   uint8_t* mask = nullptr;
   float2* normal = nullptr;

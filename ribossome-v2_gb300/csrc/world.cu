@@ -247,7 +247,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   const size_t M = build_levels((int)c.fluid_w, (int)c.fluid_h, c.mg_min_size ? c.mg_min_size : 8, lv);
   size_t b = 0;
   b += C * (16 + 16 + 4 + 8 + 4 + 4);                             // chem a/b, gamma, slope, agg_act, agg_nb
-  b += C * (1 + 4) + 16;                                          // terrain move codes, eviction list, count
+  b += 2 * C + terrain_list_entries((int)c.grid_w, (int)c.grid_h) * 4 + 64;  // terrain codes, arrivals, lists, counts
   b += 2 * L * 4 * 3;                                             // light, light_next, shade
   b += F * (1 + 8 + 4 + 8 * 3 + 4 * 3 + 4 * 5 + 8 * 3 + 4 + 4);  // mask..heat, mask32, p_tmp
   b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 * 2 + MAX_STEPS * 12 * 4 + 16;
@@ -287,8 +287,9 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(agg_act, C * 4);
   RB_ALLOC(agg_nb, C * 4);
   RB_ALLOC(terrain_code, C);
-  RB_ALLOC(terrain_list, C * 4);
-  RB_ALLOC(terrain_count, 16);
+  RB_ALLOC(terrain_arrivals, C);
+  RB_ALLOC(terrain_list, terrain_list_entries(gw, gh) * 4);
+  RB_ALLOC(terrain_count, 64);
   RB_ALLOC(mask, F);
   RB_ALLOC(normal, F * 8);
   RB_ALLOC(curl, F * 4);

@@ -127,7 +127,8 @@ def test_world_footprint_counts_every_buffer(rw):
                 nx, ny = nx // 2, ny // 2
             else:
                 break
-        want = C * 57 + 24 * L + F * 101 + (fw + fh) * 4 + 96 + 64 * 48 + 32 + M * 13 + 2 * 64 * 464
+        terrain = 2 * C + 36 * ((gw + 2) // 3) * ((gh + 2) // 3) + 64
+        want = C * 52 + terrain + 24 * L + F * 101 + (fw + fh) * 4 + 96 + 64 * 48 + 16 + M * 13 + 2 * 64 * 464
         assert rw.world_footprint((gw, gh), (fw, fh), mg_min_size=mg) == want
 
 
