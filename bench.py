@@ -663,7 +663,35 @@ def run_terrain(args):
         "matter_conserved": [led.channel(c) for c in range(4)] == [seeded.channel(c) for c in range(4)],
     }
     del w
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = terrain_cpu_sample(n)
     return out
+
+
+def terrain_cpu_sample(n, m=512, passes=8):
+    """The oracle's terrain passes (relax a, relax b, grain_fall) on the host
+    cores: a bounded sample on an m x m world of the same inputs, scaled to
+    the n x n world by cells."""
+    import ribo_oracle
+    import ribo_world as rw
+    import synth
+
+    ribo_oracle.set_threads(os.cpu_count() or 1)
+    o = ribo_oracle.OracleWorld(m, seed=1001)
+    o.seed_inputs(synth.make_world_inputs(m, seed=1001, rubble_frac=0.1))
+    bp = synth.bench_params(1001)
+    for k, _ in rw.SimParams._fields_:
+        setattr(o.params, k, getattr(bp, k))
+    o.params.sediment_settle = 0.5
+    o.settings.terrain_mode = 1
+    t = time.perf_counter()
+    for e in range(passes):
+        o.params.epoch = e
+        for which in (16, 17, 18):
+            o.run_pass(o.params, which)
+    el = time.perf_counter() - t
+    return {"terrain_ms_per_step": el / passes * 1e3 * (n * n) / (m * m), "cores": ribo_oracle.get_threads(),
+            "kind": "port", "sample": f"{passes} terrain blocks of a {m}x{m} world ({el:.2f} s), scaled by cells"}
 
 
 def run_mixed(args, local):
