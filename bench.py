@@ -28,6 +28,8 @@ transport + ledger) of one world.
          relative residual of 1e-5 every step; residual re-checked in FP64
   --ncu-case   seed the world and run --steps steps with nothing else (a
          short program for ncu captures; prints nothing)
+  --ncu-terrain  the same with the terrain block on (10% rubble, grains
+         settling), for captures of the terrain kernels
 N > 1 GPUs run independent replicas (one world per rank, no collective).
 """
 import argparse
@@ -888,9 +890,10 @@ def main():
     ap.add_argument("--serve-sustainable-rate", type=float, default=6.0)
     ap.add_argument("--serve-sustainable-seconds", type=float, default=40.0)
     ap.add_argument("--ncu-case", action="store_true")
+    ap.add_argument("--ncu-terrain", action="store_true")
     ap.add_argument("--ncu-mixed", action="store_true")
     args = ap.parse_args()
-    if args.ncu_case:
+    if args.ncu_case or args.ncu_terrain:
         import ribo_world as rw
         import synth
 
@@ -898,8 +901,12 @@ def main():
                      precision_mode=1 if args.ncu_mixed else 0)
         w.settings.fluid_substep = 1
         w.settings.mg_cycles = 4
-        w.seed_inputs(synth.make_world_inputs(args.size, seed=1000))
+        w.seed_inputs(synth.make_world_inputs(args.size, seed=1000 if not args.ncu_terrain else 1001,
+                                              rubble_frac=0.1 if args.ncu_terrain else 0.0))
         w.params = synth.bench_params(1000)
+        if args.ncu_terrain:
+            w.settings.terrain_mode = 1
+            w.params.sediment_settle = 0.5
         w.run(args.steps)
         w.sync()
         return

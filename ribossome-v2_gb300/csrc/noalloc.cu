@@ -129,7 +129,7 @@ extern "C" ribo_status ribo_pressure_solve_noalloc(uint32_t fluid_w, uint32_t fl
   uint32_t* status = reinterpret_cast<uint32_t*>(take(4));
   if (at > NOALLOC_SCRATCH_BYTES) return set_error(RIBO_INVALID_ARG, "scratch layout overflow");
 
-  Dev d;
+  Dev d{};
   memset(&d, 0, sizeof d);
   d.fw = d.gw = (int)fluid_w;
   d.fh = d.gh = (int)fluid_h;

@@ -76,6 +76,7 @@ struct Dev {
   float sx, sy;  // f32(GRID) / f32(FLUID)
   float sim_w, sim_h, cell_w;
   float wpf_x, wpf_y;  // SIM_SIZE / f32(FLUID_SIZE)
+  int pad0;            // explicit, zero: Dev records are compared byte for byte (batch tables)
   // environment-resolution buffers
   uint32_t* chem;       // chem_grid (state before the step)
   uint32_t* chem_next;  // transport destination (zero between steps)
@@ -109,6 +110,7 @@ struct Dev {
   uint8_t* fluid0;    // level-0 water flags of the multigrid (1 = water), rebuilt with the mask
   uint32_t* status;   // error bits written by kernels instead of trapping (RIBO_ERR_*)
 };
+static_assert(sizeof(Dev) == 16 * 4 + 30 * sizeof(void*), "Dev has no padding bytes: every byte is a member");
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }

@@ -145,7 +145,7 @@ void* World::field_ptr(ribo_field f) {
 }
 
 Dev World::dev() const {
-  Dev d;
+  Dev d{};  // every byte set: batches key their tables on Dev records
   d.gw = gw;
   d.gh = gh;
   d.fw = fw;
