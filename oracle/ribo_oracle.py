@@ -240,7 +240,14 @@ def _default_params(seed: int = 1) -> "rw.SimParams":
 
 
 def _default_settings() -> "rw.WorldSettings":
-    return rw.WorldSettings(1, 2, 1, 1, 128)
+    """src/world/mod.rs:117-134: fluid on, substep 2, multigrid with one
+    V-cycle, 128 Jacobi iterations, the light propagating one row per step
+    with full sweeps every 10 steps when it does not; the light and the
+    terrain stay frozen inputs unless a test turns their blocks on."""
+    s = rw.WorldSettings(1, 2, 1, 1, 128)
+    s.light_rows_per_step = 1
+    s.light_interval = 10
+    return s
 
 
 default_params = _default_params

@@ -172,25 +172,24 @@ __global__ void k_add_forces(const __grid_constant__ S s, int dir) {
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   const int fw = d.fw;
   size_t idx = (size_t)y * fw + x;
-  if (is_solid(d, x, y)) {
-    vout[idx] = f2(0.0f, 0.0f);
-    return;
-  }
+  // every load issued before any selection (the wall test included)
+  const uint8_t mc = __ldg(d.mask + idx);
+  const float2 vc = __ldg(vin + idx), n = __ldg(d.normal + idx);
   const float dt = fluid_dt(P);
   uint32_t xm = x > 0u ? x - 1u : x, xp = x + 1u < (uint32_t)fw ? x + 1u : x;
   uint32_t ym = y > 0u ? y - 1u : y, yp = y + 1u < (uint32_t)d.fh ? y + 1u : y;
-  auto F = [&](uint32_t a, uint32_t b) { return sanitize(d.forces[(size_t)b * fw + a]); };
+  auto F = [&](uint32_t a, uint32_t b) { return sanitize(__ldg(d.forces + (size_t)b * fw + a)); };
   float2 f_c = F(x, y);
   float2 axis = add2(add2(add2(F(xm, y), F(xp, y)), F(x, ym)), F(x, yp));
   float2 diag = add2(add2(add2(F(xm, ym), F(xp, ym)), F(xm, yp)), F(xp, yp));
   float2 f_avg = mul2(add2(add2(smul2(4.0f, axis), diag), smul2(20.0f, f_c)), (float)(1.0 / 36.0));
   float2 f_user = clamp_len(mix2(f_c, f_avg, FORCE_SMOOTH_MIX), MAX_FORCE);
-  float2 v = sanitize(add2(sanitize(vin[idx]), mul2(f_user, dt)));
+  float2 v = sanitize(add2(sanitize(vc), mul2(f_user, dt)));
   v = slope_steer(d, P, x, y, v, dt);
   const float drag = rubble_drag(d, x, y, dt);
   if (drag != 1.0f) v = mul2(v, drag);  // v * 1 is v
-  v = reflect_if_into_solid(d, x, y, v);
-  vout[idx] = clamp_len(v, MAX_VEL);
+  v = reflect_stored(n, v);
+  vout[idx] = mc ? f2(0.0f, 0.0f) : clamp_len(v, MAX_VEL);
 }
 
 // fluid.wgsl:435-456
@@ -201,27 +200,31 @@ __global__ void k_diffuse(const __grid_constant__ S s, int dir) {
   float2* __restrict__ vout = dir ? d.va : d.vb;
   uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
-  size_t idx = (size_t)y * d.fw + x;
-  if (is_solid(d, x, y)) {
-    vout[idx] = f2(0.0f, 0.0f);
-    return;
+  const size_t fw = (size_t)d.fw, idx = (size_t)y * fw + x;
+  const bool border = x == 0u || x == (uint32_t)d.fw - 1u || y == 0u || y == (uint32_t)d.fh - 1u;
+  // the 3 x 3 block (clamped at the border, where the result is the copy)
+  const size_t cl = x > 0u ? 1 : 0, cr = x + 1u < (uint32_t)d.fw ? 1 : 0;
+  const size_t rb = y > 0u ? fw : 0, rt = y + 1u < (uint32_t)d.fh ? fw : 0;
+  const size_t at[9] = {idx, idx - cl, idx + cr, idx - rb, idx + rt, idx - rb - cl, idx - rb + cr, idx + rt - cl, idx + rt + cr};
+  uint8_t m[9];
+  float2 v[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    m[k] = __ldg(d.mask + at[k]);
+    v[k] = __ldg(vin + at[k]);
   }
-  if (x == 0u || x == (uint32_t)d.fw - 1u || y == 0u || y == (uint32_t)d.fh - 1u) {
-    vout[idx] = vin[idx];
-    return;
-  }
-  float2 v_c = raw_velocity_cell(d, vin, x, y);
-  float2 axis_sum = add2(add2(add2(raw_velocity_cell(d, vin, x - 1, y), raw_velocity_cell(d, vin, x + 1, y)),
-                              raw_velocity_cell(d, vin, x, y - 1)),
-                         raw_velocity_cell(d, vin, x, y + 1));
-  float2 diag_sum = add2(add2(add2(raw_velocity_cell(d, vin, x - 1, y - 1), raw_velocity_cell(d, vin, x + 1, y - 1)),
-                              raw_velocity_cell(d, vin, x - 1, y + 1)),
-                         raw_velocity_cell(d, vin, x + 1, y + 1));
-  float2 lap = mul2(sub2(add2(smul2(4.0f, axis_sum), diag_sum), smul2(20.0f, v_c)), (float)(1.0 / 6.0));
-  float a = rb_max(P->fluid_viscosity, 0.0f) * fluid_dt(P);
-  float2 v = sanitize(add2(v_c, smul2(a, lap)));
-  v = reflect_if_into_solid(d, x, y, v);
-  vout[idx] = clamp_len(v, MAX_VEL);
+  const float2 n = __ldg(d.normal + idx);
+  float2 r[9];  // raw_velocity_cell
+#pragma unroll
+  for (int k = 0; k < 9; k++) r[k] = m[k] ? f2(0.0f, 0.0f) : sanitize(v[k]);
+  const float2 v_c = r[0];
+  const float2 axis_sum = add2(add2(add2(r[1], r[2]), r[3]), r[4]);
+  const float2 diag_sum = add2(add2(add2(r[5], r[6]), r[7]), r[8]);
+  const float2 lap = mul2(sub2(add2(smul2(4.0f, axis_sum), diag_sum), smul2(20.0f, v_c)), (float)(1.0 / 6.0));
+  const float a = rb_max(P->fluid_viscosity, 0.0f) * fluid_dt(P);
+  float2 vv = sanitize(add2(v_c, smul2(a, lap)));
+  vv = reflect_stored(n, vv);
+  vout[idx] = m[0] ? f2(0.0f, 0.0f) : (border ? v[0] : clamp_len(vv, MAX_VEL));
 }
 
 // fluid.wgsl:226-255
@@ -257,20 +260,18 @@ __global__ void k_advect(const __grid_constant__ S s, int dir) {
   uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
-  if (is_solid(d, x, y)) {
-    vout[idx] = f2(0.0f, 0.0f);
-    return;
-  }
+  // the cell's own loads together, the wall test at the end
+  const uint8_t mc = __ldg(d.mask + idx);
+  const float2 vc = __ldg(vin + idx), n = __ldg(d.normal + idx);
   const float dt = fluid_dt(P);
   const float decay_factor = decay_shared;
-  const float2 n = d.normal[idx];
   float2 pos = f2((float)x + 0.5f, (float)y + 0.5f);
-  float2 vel = reflect_stored(n, clamp_len(raw_velocity_cell(d, vin, x, y), MAX_VEL));
+  float2 vel = reflect_stored(n, clamp_len(sanitize(vc), MAX_VEL));  // raw_velocity_cell of a water cell
   float2 trace_pos = sub2(pos, mul2(vel, dt));
   if (is_solid_at_pos(d, trace_pos)) trace_pos = sub2(pos, mul2(reflect_stored(n, vel), dt));
   float2 out_v = sanitize(mul2(sample_velocity(d, vin, trace_pos), decay_factor));
   out_v = reflect_stored(n, out_v);
-  vout[idx] = clamp_len(out_v, MAX_VEL);
+  vout[idx] = mc ? f2(0.0f, 0.0f) : clamp_len(out_v, MAX_VEL);
 }
 
 // fluid.wgsl:479-518
@@ -299,58 +300,54 @@ __global__ void k_vorticity(const __grid_constant__ S s, int dir) {
   float2* __restrict__ vout = dir ? d.va : d.vb;
   uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
-  size_t idx = (size_t)y * d.fw + x;
-  if (is_solid(d, x, y)) {
-    vout[idx] = f2(0.0f, 0.0f);
-    return;
-  }
+  const size_t fw = (size_t)d.fw, idx = (size_t)y * fw + x;
   const float epsilon = rb_clamp(P->fluid_vorticity, 0.0f, 10.0f);
   const uint32_t border = 2u;
-  if (x < border || x >= (uint32_t)d.fw - border || y < border || y >= (uint32_t)d.fh - border || epsilon < (float)1e-6) {
-    vout[idx] = vin[idx];
-    return;
-  }
+  const bool copy = x < border || x >= (uint32_t)d.fw - border || y < border || y >= (uint32_t)d.fh - border ||
+                    epsilon < (float)1e-6;
   // curl_at of this cell and its 4 neighbours, precomputed once per cell by
-  // k_curl (the same function of the same inputs, so the same bits)
-  const float* cu = d.curl;
-  const int fw = d.fw;
-  float w = cu[idx];
-  if (rb_abs(w) < (float)5e-4) {
-    vout[idx] = vin[idx];
-    return;
-  }
-  float2 grad = mul2(f2(rb_abs(cu[idx + 1]) - rb_abs(cu[idx - 1]), rb_abs(cu[idx + fw]) - rb_abs(cu[idx - fw])), 0.5f);
+  // k_curl (the same function of the same inputs, so the same bits); the
+  // neighbour addresses are clamped where the cell is copied anyway
+  const size_t il = x > 0u ? idx - 1 : idx, ir = x + 1u < (uint32_t)d.fw ? idx + 1 : idx;
+  const size_t ib = y > 0u ? idx - fw : idx, it = y + 1u < (uint32_t)d.fh ? idx + fw : idx;
+  const float* __restrict__ cu = d.curl;
+  const uint8_t mc = __ldg(d.mask + idx);
+  const float w = __ldg(cu + idx), cl = __ldg(cu + il), cr = __ldg(cu + ir), cb = __ldg(cu + ib), ct = __ldg(cu + it);
+  const float2 vc = __ldg(vin + idx), n_wall = __ldg(d.normal + idx);
+  float2 grad = mul2(f2(rb_abs(cr) - rb_abs(cl), rb_abs(ct) - rb_abs(cb)), 0.5f);
   float2 n = div2(grad, rb_max(len2(grad), (float)1e-5));
   float2 f = mul2(f2(n.y, -n.x), w * epsilon);
   float2 dv = clamp_len(mul2(f, fluid_dt(P)), 2.0f);
-  float2 v = sanitize(add2(vin[idx], dv));
-  v = reflect_if_into_solid(d, x, y, v);
-  vout[idx] = clamp_len(v, MAX_VEL);
+  float2 v = sanitize(add2(vc, dv));
+  v = reflect_stored(n_wall, v);
+  vout[idx] = mc ? f2(0.0f, 0.0f) : ((copy || rb_abs(w) < (float)5e-4) ? vc : clamp_len(v, MAX_VEL));
 }
 
 // fluid.wgsl:520-551
-__device__ __forceinline__ float2 div_neighbor(const Dev& d, const float2* vin, float2 v_c, int nx, int ny, bool axis_x) {
-  bool outside = nx < 0 || ny < 0 || nx >= d.fw || ny >= d.fh;
-  if (outside || is_solid(d, nx, ny)) return axis_x ? f2(-v_c.x, v_c.y) : f2(v_c.x, -v_c.y);
-  return raw_velocity_cell(d, vin, nx, ny);
-}
+// The stencil passes below issue every global load of a cell first (border
+// neighbours clamped to the cell itself, so every address is in the grid)
+// and select afterwards: one load latency per cell instead of a chain of
+// mask -> neighbour mask -> value.  A wall cell's value is computed and
+// discarded; a water cell's is the same expression as the branching form.
 template <class S>
 __global__ void k_divergence(const __grid_constant__ S s, int dir) {
   RB_WORLD(s);
   const float2* __restrict__ vin = dir ? d.vb : d.va;
   int x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= d.fw || y >= d.fh) return;
-  size_t idx = (size_t)y * d.fw + x;
-  if (is_solid(d, x, y)) {
-    d.div[idx] = 0.0f;
-    return;
-  }
-  float2 v_c = raw_velocity_cell(d, vin, x, y);
-  float2 v_l = div_neighbor(d, vin, v_c, x - 1, y, true);
-  float2 v_r = div_neighbor(d, vin, v_c, x + 1, y, true);
-  float2 v_b = div_neighbor(d, vin, v_c, x, y - 1, false);
-  float2 v_t = div_neighbor(d, vin, v_c, x, y + 1, false);
-  d.div[idx] = 0.5f * ((v_r.x - v_l.x) + (v_t.y - v_b.y));
+  const size_t fw = (size_t)d.fw, idx = (size_t)y * fw + x;
+  const bool hl = x > 0, hr = x + 1 < d.fw, hb = y > 0, ht = y + 1 < d.fh;
+  const size_t il = hl ? idx - 1 : idx, ir = hr ? idx + 1 : idx, ib = hb ? idx - fw : idx, it = ht ? idx + fw : idx;
+  const uint8_t mc = __ldg(d.mask + idx), ml = __ldg(d.mask + il), mr = __ldg(d.mask + ir);
+  const uint8_t mb = __ldg(d.mask + ib), mt = __ldg(d.mask + it);
+  const float2 vc = __ldg(vin + idx), vl = __ldg(vin + il), vr = __ldg(vin + ir), vb = __ldg(vin + ib), vt = __ldg(vin + it);
+  // div_neighbor: the border or a wall mirrors the cell's own velocity
+  const float2 v_c = sanitize(vc);
+  const float2 v_l = (!hl || ml) ? f2(-v_c.x, v_c.y) : sanitize(vl);
+  const float2 v_r = (!hr || mr) ? f2(-v_c.x, v_c.y) : sanitize(vr);
+  const float2 v_b = (!hb || mb) ? f2(v_c.x, -v_c.y) : sanitize(vb);
+  const float2 v_t = (!ht || mt) ? f2(v_c.x, -v_c.y) : sanitize(vt);
+  d.div[idx] = mc ? 0.0f : 0.5f * ((v_r.x - v_l.x) + (v_t.y - v_b.y));
 }
 
 // fluid.wgsl:610-630
@@ -361,23 +358,21 @@ __global__ void k_subtract_gradient(const __grid_constant__ S s, int dir) {
   float2* __restrict__ vout = dir ? d.va : d.vb;
   uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
-  const int fw = d.fw;
-  size_t idx = (size_t)y * fw + x;
-  if (is_solid(d, x, y)) {
-    vout[idx] = f2(0.0f, 0.0f);
-    return;
-  }
-  const float* p = d.pa;
-  float p_c = p[idx];
-  float p_l = p_c, p_r = p_c, p_b = p_c, p_t = p_c;
-  if (x > 0u && !is_solid(d, x - 1, y)) p_l = p[idx - 1];
-  if (x + 1u < (uint32_t)fw && !is_solid(d, x + 1, y)) p_r = p[idx + 1];
-  if (y > 0u && !is_solid(d, x, y - 1)) p_b = p[idx - fw];
-  if (y + 1u < (uint32_t)d.fh && !is_solid(d, x, y + 1)) p_t = p[idx + fw];
+  const size_t fw = (size_t)d.fw, idx = (size_t)y * fw + x;
+  const bool hl = x > 0u, hr = x + 1u < (uint32_t)d.fw, hb = y > 0u, ht = y + 1u < (uint32_t)d.fh;
+  const size_t il = hl ? idx - 1 : idx, ir = hr ? idx + 1 : idx, ib = hb ? idx - fw : idx, it = ht ? idx + fw : idx;
+  const float* __restrict__ p = d.pa;
+  const uint8_t mc = __ldg(d.mask + idx), ml = __ldg(d.mask + il), mr = __ldg(d.mask + ir);
+  const uint8_t mb = __ldg(d.mask + ib), mt = __ldg(d.mask + it);
+  const float p_c = __ldg(p + idx), pl = __ldg(p + il), pr = __ldg(p + ir), pb = __ldg(p + ib), pt = __ldg(p + it);
+  const float2 vc = __ldg(vin + idx), n = __ldg(d.normal + idx);
+  // a wall or the border neighbour takes the cell's own pressure
+  const float p_l = (hl && !ml) ? pl : p_c, p_r = (hr && !mr) ? pr : p_c;
+  const float p_b = (hb && !mb) ? pb : p_c, p_t = (ht && !mt) ? pt : p_c;
   float2 grad = mul2(f2(p_r - p_l, p_t - p_b), 0.5f);
-  float2 v = sub2(sanitize(vin[idx]), grad);
-  v = reflect_if_into_solid(d, x, y, v);
-  vout[idx] = clamp_len(sanitize(v), MAX_VEL);
+  float2 v = sub2(sanitize(vc), grad);
+  v = reflect_stored(n, v);
+  vout[idx] = mc ? f2(0.0f, 0.0f) : clamp_len(sanitize(v), MAX_VEL);
 }
 
 // fluid.wgsl:640-657.  The reference sums each row (column) serially in
@@ -476,16 +471,15 @@ __global__ void k_boundaries(const __grid_constant__ S s, int dir) {
   uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   size_t idx = (size_t)y * d.fw + x;
-  if (is_solid(d, x, y)) {
-    vout[idx] = f2(0.0f, 0.0f);
-    return;
-  }
-  float2 v = sanitize(vin[idx]);
-  v = sub2(v, f2(d.net_flux[d.fh + x], d.net_flux[y]));
+  const uint8_t mc = __ldg(d.mask + idx);
+  const float2 vc = __ldg(vin + idx), n = __ldg(d.normal + idx);
+  const float fx = __ldg(d.net_flux + d.fh + x), fy = __ldg(d.net_flux + y);
+  float2 v = sanitize(vc);
+  v = sub2(v, f2(fx, fy));
   if (x == 0u || x == (uint32_t)d.fw - 1u) v.x = 0.0f;
   if (y == 0u || y == (uint32_t)d.fh - 1u) v.y = 0.0f;
-  v = reflect_if_into_solid(d, x, y, v);
-  vout[idx] = clamp_len(sanitize(v), MAX_VEL);
+  v = reflect_stored(n, v);
+  vout[idx] = mc ? f2(0.0f, 0.0f) : clamp_len(sanitize(v), MAX_VEL);
 }
 
 // fluid.wgsl:680-693

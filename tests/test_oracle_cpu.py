@@ -196,3 +196,20 @@ def test_multigrid_level_rule(ro, n, levels):
         while sizes[-1] > 16 and sizes[-1] % 2 == 0:
             sizes.append(sizes[-1] // 2)
         assert len(sizes) == levels
+
+
+def test_oracle_default_settings_match_the_library(rw, ro):
+    """Both sides start from the reference's WorldSettings defaults
+    (src/world/mod.rs:117-134), so a test that sets only some fields compares
+    like with like (the mixed-solver fields, which the oracle does not run,
+    take their defaults from zero)."""
+    import ctypes
+
+    lib = rw.load_library()
+    want = rw.WorldSettings()
+    lib.ribo_world_settings_default(ctypes.byref(want))
+    got = ro._default_settings()
+    for name, _ in rw.WorldSettings._fields_:
+        if name.startswith("mixed_"):
+            continue
+        assert getattr(got, name) == getattr(want, name), name
