@@ -54,7 +54,22 @@ __global__ void k_temperature(const __grid_constant__ S s) {
   const int fw = d.fw, fh = d.fh;
   size_t idx = (size_t)y * fw + x;
   const float dt = fluid_dt(P);
-  float2 vel = raw_velocity_cell(d, d.va, x, y);
+  const float* __restrict__ T = d.temp_in;   // temp_out and redox_out are the other buffers
+  const float* __restrict__ R = d.redox_in;
+  // the loads that do not depend on the velocity go out with it; only the
+  // two bilinear gathers wait for it
+  const uint8_t solid = __ldg(d.mask + idx);
+  const float2 v_raw = __ldg(d.va + idx);
+  uint32_t xl = x > 0u ? x - 1u : 0u, xr = umin(x + 1u, (uint32_t)fw - 1u);
+  uint32_t yb = y > 0u ? y - 1u : 0u, yt = umin(y + 1u, (uint32_t)fh - 1u);
+  const float tl = __ldg(T + (size_t)y * fw + xl), tr = __ldg(T + (size_t)y * fw + xr);
+  const float tb = __ldg(T + (size_t)yb * fw + x), tt = __ldg(T + (size_t)yt * fw + x);
+  const float rl = __ldg(R + (size_t)y * fw + xl), rr = __ldg(R + (size_t)y * fw + xr);
+  const float rbt = __ldg(R + (size_t)yb * fw + x), rt = __ldg(R + (size_t)yt * fw + x);
+  const float2 h = __ldg(d.heat + idx);
+  const uint32_t eaten = d.redox_eaten[idx];
+  const float fill = gamma_fill_at_fluid_cell(d, x, y);
+  float2 vel = solid ? f2(0.0f, 0.0f) : sanitize(v_raw);  // raw_velocity_cell
   float srcx = ((float)x + 0.5f) - vel.x * dt;
   float srcy = ((float)y + 0.5f) - vel.y * dt;
   float sxf = rb_clamp(srcx - 0.5f, 0.0f, (float)(fw - 1));
@@ -62,15 +77,12 @@ __global__ void k_temperature(const __grid_constant__ S s) {
   uint32_t x0 = rb_f2u(rb_floor(sxf)), y0 = rb_f2u(rb_floor(syf));
   uint32_t x1 = umin(x0 + 1u, (uint32_t)fw - 1u), y1 = umin(y0 + 1u, (uint32_t)fh - 1u);
   float fx = rb_fract(sxf), fy = rb_fract(syf);
-  const float* T = d.temp_in;
-  float t = rb_mix(rb_mix(T[(size_t)y0 * fw + x0], T[(size_t)y0 * fw + x1], fx),
-                   rb_mix(T[(size_t)y1 * fw + x0], T[(size_t)y1 * fw + x1], fx), fy);
-  uint32_t xl = x > 0u ? x - 1u : 0u, xr = umin(x + 1u, (uint32_t)fw - 1u);
-  uint32_t yb = y > 0u ? y - 1u : 0u, yt = umin(y + 1u, (uint32_t)fh - 1u);
-  float tl = T[(size_t)y * fw + xl], tr = T[(size_t)y * fw + xr], tb = T[(size_t)yb * fw + x], tt = T[(size_t)yt * fw + x];
-  float fill = gamma_fill_at_fluid_cell(d, x, y);
+  const float t00 = __ldg(T + (size_t)y0 * fw + x0), t01 = __ldg(T + (size_t)y0 * fw + x1);
+  const float t10 = __ldg(T + (size_t)y1 * fw + x0), t11 = __ldg(T + (size_t)y1 * fw + x1);
+  const float r00 = __ldg(R + (size_t)y0 * fw + x0), r01 = __ldg(R + (size_t)y0 * fw + x1);
+  const float r10 = __ldg(R + (size_t)y1 * fw + x0), r11 = __ldg(R + (size_t)y1 * fw + x1);
+  float t = rb_mix(rb_mix(t00, t01, fx), rb_mix(t10, t11, fx), fy);
   t = rb_mix(t, (tl + tr + tb + tt) * 0.25f, TEMP_DIFFUSE * rb_mix(1.0f, TEMP_ROCK_CONDUCT, fill));
-  const float2 h = d.heat[idx];
   // The vent cycle only scales vent heat.  It is finite and >= +0 for a
   // finite amplitude, so with no heat here both products are zeros of the
   // heat's signs whatever its value, and the sine is not evaluated.
@@ -89,13 +101,10 @@ __global__ void k_temperature(const __grid_constant__ S s) {
   else t = amb + (t - amb) * rb_exp(-TEMP_COOL_RATE * (1.0f - fill) * dt);
   d.temp_out[idx] = rb_clamp(t, 0.0f, TEMP_MAX);
 
-  const float* R = d.redox_in;
-  float r = rb_mix(rb_mix(R[(size_t)y0 * fw + x0], R[(size_t)y0 * fw + x1], fx),
-                   rb_mix(R[(size_t)y1 * fw + x0], R[(size_t)y1 * fw + x1], fx), fy);
-  float rl = R[(size_t)y * fw + xl], rr = R[(size_t)y * fw + xr], rbt = R[(size_t)yb * fw + x], rt = R[(size_t)yt * fw + x];
+  float r = rb_mix(rb_mix(r00, r01, fx), rb_mix(r10, r11, fx), fy);
   r = rb_mix(r, (rl + rr + rbt + rt) * 0.25f, TEMP_DIFFUSE);
   r += h.y * vc * REDOX_RATE * dt;
-  r = rb_max(r - (float)d.redox_eaten[idx] / REDOX_FP, 0.0f);
+  r = rb_max(r - (float)eaten / REDOX_FP, 0.0f);
   // a zero times a finite factor in [0, 1] keeps its sign: skip the exponential
   const float decay_arg = -rb_max(P->redox_decay, 0.0f) * dt;
   if (r != 0.0f || !(decay_arg <= 0.0f)) r *= rb_exp(decay_arg);
