@@ -386,10 +386,11 @@ __global__ void k_subtract_gradient(const __grid_constant__ S s, int dir) {
 
 // fluid.wgsl:640-657.  The reference sums each row (column) serially in
 // f32; the order of those adds fixes the rounding, so each line is summed
-// by one lane in index order.  A block owns 32 lines: its warps 1..7 stream
+// by one lane in index order.  A block owns 32 lines: its warps 1..15 stream
 // chunks of NF_C elements of those lines into a double-buffered shared
 // tile, while warp 0 (lane = line) runs the 32 serial add chains over the
-// previous chunk.  A chunk is NF_C units of one coalesced warp load (32
+// previous chunk (the double buffer lives in dynamic shared memory).  A
+// chunk is NF_C units of one coalesced warp load (32
 // cells of a row, or one position of the 32 columns); a loader warp issues
 // all its units' loads before storing any, so a chunk costs about one load
 // latency.  Wall cells are stored as +0.0: the running sum starts at +0.0
@@ -397,7 +398,8 @@ __global__ void k_subtract_gradient(const __grid_constant__ S s, int dir) {
 // unchanged, and the chain needs no branch; the water cells are counted
 // separately (the reference's n, an exact integer in f32).  Row blocks and
 // column blocks share one launch.
-constexpr int NF_L = NET_FLUX_LINES, NF_C = 128, NF_THREADS = 256;
+constexpr int NF_L = NET_FLUX_LINES, NF_C = 256, NF_THREADS = 512;
+constexpr size_t NF_SMEM = (size_t)2 * NF_L * (NF_C + 1) * sizeof(float);
 constexpr int NF_LOADERS = NF_THREADS / 32 - 1, NF_UPW = (NF_C + NF_LOADERS - 1) / NF_LOADERS;
 static_assert(NF_L == 32 && NF_C % 32 == 0, "a unit is one warp load");
 template <class S>
@@ -406,7 +408,8 @@ __global__ void __launch_bounds__(NF_THREADS) k_net_flux(const __grid_constant__
   const float2* __restrict__ vin = dir ? d.vb : d.va;
   const uint8_t* __restrict__ mask = d.mask;
   const int row_blocks = (d.fh + NF_L - 1) / NF_L;
-  __shared__ float val[2][NF_L][NF_C + 1];
+  extern __shared__ float nf_smem[];
+  float(*val)[NF_L][NF_C + 1] = reinterpret_cast<float(*)[NF_L][NF_C + 1]>(nf_smem);
   __shared__ uint32_t wet_cells[NF_L];
   const bool rows = (int)cta.bx < row_blocks;
   const int line0 = (rows ? (int)cta.bx : (int)cta.bx - row_blocks) * NF_L;
@@ -541,7 +544,15 @@ void launch_subtract_gradient(const Target& t, int dir, cudaStream_t s) {
   RB_PASS("subtract_gradient", 21.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_subtract_gradient, nullptr, dir);
 }
 void launch_net_flux(const Target& t, int dir, cudaStream_t s) {
-  RB_PASS("net_flux", 18.0 * t.fcells, s, t, GEO_NET_FLUX, dim3(NF_THREADS), 0, k_net_flux, nullptr, dir);
+  static uint64_t attr_done = 0;  // one bit per device: the double buffer is above the 48 KB default
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!(attr_done >> (dev & 63) & 1ull)) {
+    cudaFuncSetAttribute(k_net_flux<OneWorld>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NF_SMEM);
+    cudaFuncSetAttribute(k_net_flux<WorldSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NF_SMEM);
+    attr_done |= 1ull << (dev & 63);
+  }
+  RB_PASS("net_flux", 18.0 * t.fcells, s, t, GEO_NET_FLUX, dim3(NF_THREADS), NF_SMEM, k_net_flux, nullptr, dir);
 }
 void launch_boundaries(const Target& t, int dir, cudaStream_t s) {
   RB_PASS("enforce_boundaries", 17.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_boundaries, nullptr, dir);
