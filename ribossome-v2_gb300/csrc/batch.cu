@@ -49,6 +49,10 @@ void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby) {
       *nbx = (d.lw + PASS_BX - 1) / PASS_BX;
       *nby = (d.lh + PASS_BY - 1) / PASS_BY;
       return;
+    case GEO_FLUID_TALL:
+      *nbx = (d.fw + PASS_BX - 1) / PASS_BX;
+      *nby = (d.fh + PASS_BY * FLUID_ROWS - 1) / (PASS_BY * FLUID_ROWS);
+      return;
     case GEO_LEDGER: {
       long long b = (cells + LEDGER_CELLS_PER_CTA - 1) / LEDGER_CELLS_PER_CTA;
       *nbx = (int)(b < 1 ? 1 : (b > 152 * 8 ? 152 * 8 : b));

@@ -123,23 +123,38 @@ __device__ __forceinline__ uint32_t quant_force(float v) {
 template <class S>
 __global__ void k_forces(const __grid_constant__ S s) {
   RB_WORLD(s);
-  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
-  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
-  size_t idx = (size_t)y * d.fw + x;
-  uint2 fv = reinterpret_cast<uint2*>(d.force_vec)[idx];
-  if (!(x == 0u || y == 0u || x >= (uint32_t)d.fw - 1u || y >= (uint32_t)d.fh - 1u)) {
-    float dev = d.temp_in[idx] - temp_ambient_at(d, y);
-    if (!(rb_abs(dev) <= (float)1e-3)) {
-      uint32_t time_bucket = P->epoch / 16u;
-      float r = rb_u2f(rb_pcg4d((uint32_t)idx, time_bucket, RB_S_BUOYANCY, P->seed).x);
-      float side = (r * 2.0f - 1.0f) * 0.25f * rb_abs(dev) / rb_max(rb_abs(dev), 1.0f);
-      fv.x += quant_force(side * TEMP_BUOYANCY * rb_abs(dev));
-      fv.y += quant_force(TEMP_BUOYANCY * dev);
-    }
+  const uint32_t x = cta.bx * BX + threadIdx.x, y0 = cta.by * (BY * FLUID_ROWS) + threadIdx.y;
+  if (x >= (uint32_t)d.fw) return;
+  // FLUID_ROWS cells of the column, every load first (see k_smooth)
+  uint2 fv[FLUID_ROWS];
+  float tc[FLUID_ROWS];
+#pragma unroll
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = umin(y0 + r * BY, (uint32_t)d.fh - 1u);
+    const size_t idx = (size_t)y * d.fw + x;
+    fv[r] = reinterpret_cast<const uint2*>(d.force_vec)[idx];
+    tc[r] = d.temp_in[idx];
   }
-  float2 f = f2((float)(int32_t)fv.x / FORCE_FP, (float)(int32_t)fv.y / FORCE_FP);
-  d.forces[idx] = clamp_len(sanitize(f), MAX_FORCE);
-  reinterpret_cast<uint2*>(d.force_vec)[idx] = make_uint2(0u, 0u);
+#pragma unroll
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = y0 + r * BY;
+    if (y >= (uint32_t)d.fh) break;
+    const size_t idx = (size_t)y * d.fw + x;
+    uint2 v = fv[r];
+    if (!(x == 0u || y == 0u || x >= (uint32_t)d.fw - 1u || y >= (uint32_t)d.fh - 1u)) {
+      float dev = tc[r] - temp_ambient_at(d, y);
+      if (!(rb_abs(dev) <= (float)1e-3)) {
+        uint32_t time_bucket = P->epoch / 16u;
+        float rr = rb_u2f(rb_pcg4d((uint32_t)idx, time_bucket, RB_S_BUOYANCY, P->seed).x);
+        float side = (rr * 2.0f - 1.0f) * 0.25f * rb_abs(dev) / rb_max(rb_abs(dev), 1.0f);
+        v.x += quant_force(side * TEMP_BUOYANCY * rb_abs(dev));
+        v.y += quant_force(TEMP_BUOYANCY * dev);
+      }
+    }
+    float2 f = f2((float)(int32_t)v.x / FORCE_FP, (float)(int32_t)v.y / FORCE_FP);
+    d.forces[idx] = clamp_len(sanitize(f), MAX_FORCE);
+    reinterpret_cast<uint2*>(d.force_vec)[idx] = make_uint2(0u, 0u);
+  }
 }
 
 // fluid.wgsl:150-161
@@ -480,35 +495,66 @@ __global__ void k_boundaries(const __grid_constant__ S s, int dir) {
   RB_WORLD(s);
   const float2* __restrict__ vin = dir ? d.vb : d.va;
   float2* __restrict__ vout = dir ? d.va : d.vb;
-  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
-  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
-  size_t idx = (size_t)y * d.fw + x;
-  const uint8_t mc = __ldg(d.mask + idx);
-  const float2 vc = __ldg(vin + idx), n = __ldg(d.normal + idx);
-  const float fx = __ldg(d.net_flux + d.fh + x), fy = __ldg(d.net_flux + y);
-  float2 v = sanitize(vc);
-  v = sub2(v, f2(fx, fy));
-  if (x == 0u || x == (uint32_t)d.fw - 1u) v.x = 0.0f;
-  if (y == 0u || y == (uint32_t)d.fh - 1u) v.y = 0.0f;
-  v = reflect_stored(n, v);
-  vout[idx] = mc ? f2(0.0f, 0.0f) : clamp_len(sanitize(v), MAX_VEL);
+  const uint32_t x = cta.bx * BX + threadIdx.x, y0 = cta.by * (BY * FLUID_ROWS) + threadIdx.y;
+  if (x >= (uint32_t)d.fw) return;
+  const float fx = __ldg(d.net_flux + d.fh + x);
+  uint8_t mc[FLUID_ROWS];
+  float2 vc[FLUID_ROWS], n[FLUID_ROWS];
+  float fy[FLUID_ROWS];
+#pragma unroll
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = umin(y0 + r * BY, (uint32_t)d.fh - 1u);
+    const size_t idx = (size_t)y * d.fw + x;
+    mc[r] = __ldg(d.mask + idx);
+    vc[r] = __ldg(vin + idx);
+    n[r] = __ldg(d.normal + idx);
+    fy[r] = __ldg(d.net_flux + y);
+  }
+#pragma unroll
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = y0 + r * BY;
+    if (y >= (uint32_t)d.fh) break;
+    float2 v = sanitize(vc[r]);
+    v = sub2(v, f2(fx, fy[r]));
+    if (x == 0u || x == (uint32_t)d.fw - 1u) v.x = 0.0f;
+    if (y == 0u || y == (uint32_t)d.fh - 1u) v.y = 0.0f;
+    v = reflect_stored(n[r], v);
+    vout[(size_t)y * d.fw + x] = mc[r] ? f2(0.0f, 0.0f) : clamp_len(sanitize(v), MAX_VEL);
+  }
 }
 
 // fluid.wgsl:680-693
+// The streaming passes below take FLUID_ROWS cells of a column per thread
+// (rows BY apart) and load all of them before computing any: four cells'
+// loads in flight per thread instead of one.  Rows past the grid load the
+// last row and store nothing.
 template <class S>
 __global__ void k_smooth(const __grid_constant__ S s, int dir) {
   RB_WORLD(s);
   const float2* __restrict__ vin = dir ? d.vb : d.va;
-  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
-  if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
+  const uint32_t x = cta.bx * BX + threadIdx.x, y0 = cta.by * (BY * FLUID_ROWS) + threadIdx.y;
+  if (x >= (uint32_t)d.fw) return;
   const int fw = d.fw;
-  uint32_t xm = x > 0u ? x - 1u : x, xp = umin(x + 1u, (uint32_t)fw - 1u);
-  uint32_t ym = y > 0u ? y - 1u : y, yp = umin(y + 1u, (uint32_t)d.fh - 1u);
-  float2 v = add2(add2(add2(add2(sanitize(vin[(size_t)y * fw + x]), sanitize(vin[(size_t)y * fw + xm])),
-                             sanitize(vin[(size_t)y * fw + xp])),
-                        sanitize(vin[(size_t)ym * fw + x])),
-                   sanitize(vin[(size_t)yp * fw + x]));
-  d.vsmooth[(size_t)y * fw + x] = mul2(v, 0.2f);
+  const uint32_t xm = x > 0u ? x - 1u : x, xp = umin(x + 1u, (uint32_t)fw - 1u);
+  float2 v[FLUID_ROWS][5];
+#pragma unroll
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = umin(y0 + r * BY, (uint32_t)d.fh - 1u);
+    const uint32_t ym = y > 0u ? y - 1u : y, yp = umin(y + 1u, (uint32_t)d.fh - 1u);
+    v[r][0] = __ldg(vin + (size_t)y * fw + x);
+    v[r][1] = __ldg(vin + (size_t)y * fw + xm);
+    v[r][2] = __ldg(vin + (size_t)y * fw + xp);
+    v[r][3] = __ldg(vin + (size_t)ym * fw + x);
+    v[r][4] = __ldg(vin + (size_t)yp * fw + x);
+  }
+#pragma unroll
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = y0 + r * BY;
+    if (y >= (uint32_t)d.fh) break;
+    const float2 a = add2(add2(add2(add2(sanitize(v[r][0]), sanitize(v[r][1])), sanitize(v[r][2])), sanitize(v[r][3])),
+                          sanitize(v[r][4]));
+    d.vsmooth[(size_t)y * fw + x] = mul2(a, 0.2f);
+  }
 }
 
 }  // namespace
@@ -522,7 +568,7 @@ void launch_temperature(const Target& t, cudaStream_t s) {
   RB_PASS("update_temperature", 41.0 * t.fcells + 4.0 * t.cells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_temperature, nullptr);
 }
 void launch_forces(const Target& t, cudaStream_t s) {
-  RB_PASS("forces", 28.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_forces, nullptr);
+  RB_PASS("forces", 28.0 * t.fcells, s, t, GEO_FLUID_TALL, dim3(BX, BY), 0, k_forces, nullptr);
 }
 void launch_add_forces(const Target& t, int dir, cudaStream_t s) {
   RB_PASS("add_forces", 33.0 * t.fcells + 4.0 * t.cells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_add_forces, nullptr, dir);
@@ -555,10 +601,10 @@ void launch_net_flux(const Target& t, int dir, cudaStream_t s) {
   RB_PASS("net_flux", 18.0 * t.fcells, s, t, GEO_NET_FLUX, dim3(NF_THREADS), NF_SMEM, k_net_flux, nullptr, dir);
 }
 void launch_boundaries(const Target& t, int dir, cudaStream_t s) {
-  RB_PASS("enforce_boundaries", 17.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_boundaries, nullptr, dir);
+  RB_PASS("enforce_boundaries", 17.0 * t.fcells, s, t, GEO_FLUID_TALL, dim3(BX, BY), 0, k_boundaries, nullptr, dir);
 }
 void launch_smooth(const Target& t, int dir, cudaStream_t s) {
-  RB_PASS("smooth_velocity", 16.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_smooth, nullptr, dir);
+  RB_PASS("smooth_velocity", 16.0 * t.fcells, s, t, GEO_FLUID_TALL, dim3(BX, BY), 0, k_smooth, nullptr, dir);
 }
 
 }  // namespace ribo

@@ -292,6 +292,7 @@ enum : uint32_t { ERR_NONE = 0, ERR_TIMEOUT = 1, ERR_BOUNDS = 2 };
 // Block shapes of the passes, shared by the kernels and by the host code that
 // sizes batched launches.
 constexpr int PASS_BX = 32, PASS_BY = 8;        // per-cell passes: 32x8 cells per CTA
+constexpr int FLUID_ROWS = 4;                   // streaming fluid passes: rows of cells per thread
 constexpr int SCATTER_TX = 32, SCATTER_TY = 8;  // transport scatter tile
 constexpr int NET_FLUX_LINES = 32;              // rows or columns per net-flux CTA
 constexpr int LINEAR_THREADS = 256;             // 1-D passes over the environment cells

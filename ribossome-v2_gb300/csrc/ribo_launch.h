@@ -31,6 +31,7 @@ enum Geo : int {
   GEO_NET_FLUX,     // fluid rows then columns, NET_FLUX_LINES per CTA (1-D)
   GEO_LEDGER,       // environment cells, LEDGER_CELLS_PER_CTA per CTA (1-D)
   GEO_LIGHT,        // light grid (grid / LIGHT_DIV), PASS_BX x PASS_BY cells per CTA
+  GEO_FLUID_TALL,   // fluid grid, PASS_BX x (PASS_BY * FLUID_ROWS) cells per CTA
   GEO_COUNT
 };
 void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby);
