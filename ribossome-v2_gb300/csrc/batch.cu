@@ -53,6 +53,14 @@ void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby) {
       *nbx = (d.fw + PASS_BX - 1) / PASS_BX;
       *nby = (d.fh + PASS_BY * FLUID_ROWS - 1) / (PASS_BY * FLUID_ROWS);
       return;
+    case GEO_ENV_TALL:
+      *nbx = (d.gw + PASS_BX - 1) / PASS_BX;
+      *nby = (d.gh + PASS_BY * FLUID_ROWS - 1) / (PASS_BY * FLUID_ROWS);
+      return;
+    case GEO_ENV_LINEAR4:
+      *nbx = (int)((cells + 4 * LINEAR_THREADS - 1) / (4 * LINEAR_THREADS));
+      *nby = 1;
+      return;
     case GEO_LEDGER: {
       long long b = (cells + LEDGER_CELLS_PER_CTA - 1) / LEDGER_CELLS_PER_CTA;
       *nbx = (int)(b < 1 ? 1 : (b > 152 * 8 ? 152 * 8 : b));

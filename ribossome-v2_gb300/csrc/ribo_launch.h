@@ -32,6 +32,8 @@ enum Geo : int {
   GEO_LEDGER,       // environment cells, LEDGER_CELLS_PER_CTA per CTA (1-D)
   GEO_LIGHT,        // light grid (grid / LIGHT_DIV), PASS_BX x PASS_BY cells per CTA
   GEO_FLUID_TALL,   // fluid grid, PASS_BX x (PASS_BY * FLUID_ROWS) cells per CTA
+  GEO_ENV_TALL,     // environment grid, PASS_BX x (PASS_BY * FLUID_ROWS) cells per CTA
+  GEO_ENV_LINEAR4,  // environment cells, 4 * LINEAR_THREADS per CTA (1-D)
   GEO_COUNT
 };
 void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby);

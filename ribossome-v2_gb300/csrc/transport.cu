@@ -34,33 +34,56 @@ __global__ void k_slope(const __grid_constant__ Dev d, float upc) {
 template <class S>
 __global__ void k_thermal(const __grid_constant__ S s) {
   RB_WORLD(s);
-  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
-  if (x >= (uint32_t)d.gw || y >= (uint32_t)d.gh) return;
-  uint32_t fx = umin((x * (uint32_t)d.fw) / (uint32_t)d.gw, (uint32_t)d.fw - 1u);
-  uint32_t fy = umin((y * (uint32_t)d.fh) / (uint32_t)d.gh, (uint32_t)d.fh - 1u);
-  float t_loc = d.temp_in[(size_t)fy * d.fw + fx];
-  if (t_loc <= TEMP_ACT_THRESHOLD) return;
-  float p_act = rb_clamp(FUMAROLE_ACT_P * rb_max(P->thermal_activation, 0.0f) * (t_loc - TEMP_ACT_THRESHOLD) / TEMP_ACT_THRESHOLD, 0.0f,
-                         (float)0.9);
-  size_t idx = (size_t)y * d.gw + x;
-  uint4 c = reinterpret_cast<uint4*>(d.chem)[idx];
-  uint32_t w[4] = {c.x, c.y, c.z, c.w};
+  // FLUID_ROWS cells of a column per thread (rows BY apart), their
+  // temperatures loaded together
+  const uint32_t x = cta.bx * BX + threadIdx.x, y0 = cta.by * (BY * FLUID_ROWS) + threadIdx.y;
+  if (x >= (uint32_t)d.gw) return;
+  const uint32_t fx = umin((x * (uint32_t)d.fw) / (uint32_t)d.gw, (uint32_t)d.fw - 1u);
+  float t_loc[FLUID_ROWS];
 #pragma unroll
-  for (uint32_t ch = 0; ch < 4; ch++) {
-    uint32_t slot = (uint32_t)(idx * 4 + ch);
-    if ((w[ch] >> 16) > 0u && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_THERMAL, P->seed).x) < p_act) w[ch] += 0xFFFF0001u;
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = umin(y0 + r * BY, (uint32_t)d.gh - 1u);
+    const uint32_t fy = umin((y * (uint32_t)d.fh) / (uint32_t)d.gh, (uint32_t)d.fh - 1u);
+    t_loc[r] = __ldg(d.temp_in + (size_t)fy * d.fw + fx);
   }
-  reinterpret_cast<uint4*>(d.chem)[idx] = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+  for (int r = 0; r < FLUID_ROWS; r++) {
+    const uint32_t y = y0 + r * BY;
+    if (y >= (uint32_t)d.gh) break;
+    if (t_loc[r] <= TEMP_ACT_THRESHOLD) continue;
+    float p_act = rb_clamp(FUMAROLE_ACT_P * rb_max(P->thermal_activation, 0.0f) * (t_loc[r] - TEMP_ACT_THRESHOLD) / TEMP_ACT_THRESHOLD,
+                           0.0f, (float)0.9);
+    size_t idx = (size_t)y * d.gw + x;
+    uint4 c = reinterpret_cast<uint4*>(d.chem)[idx];
+    uint32_t w[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (uint32_t ch = 0; ch < 4; ch++) {
+      uint32_t slot = (uint32_t)(idx * 4 + ch);
+      if ((w[ch] >> 16) > 0u && rb_u2f(rb_pcg4d(slot, P->epoch, RB_S_THERMAL, P->seed).x) < p_act) w[ch] += 0xFFFF0001u;
+    }
+    reinterpret_cast<uint4*>(d.chem)[idx] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
 }
 
 // transport.wgsl:61-68
 template <class S>
 __global__ void k_agg_count(const __grid_constant__ S s) {
   RB_WORLD(s);
-  size_t i = (size_t)cta.bx * blockDim.x + threadIdx.x;
-  if (i >= (size_t)d.gw * d.gh) return;
-  uint4 c = load_cell(d.chem, i);
-  d.agg_act[i] = (c.x & CHEM_STATE_MASK) + (c.y & CHEM_STATE_MASK) + (c.z & CHEM_STATE_MASK) + (c.w & CHEM_STATE_MASK);
+  // four cells per thread, LINEAR_THREADS apart, loaded together
+  const size_t n = (size_t)d.gw * d.gh, i0 = (size_t)cta.bx * 4 * blockDim.x + threadIdx.x;
+  uint4 c[4];
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const size_t i = i0 + (size_t)r * blockDim.x;
+    c[r] = load_cell(d.chem, i < n ? i : n - 1);
+  }
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const size_t i = i0 + (size_t)r * blockDim.x;
+    if (i < n)
+      d.agg_act[i] = (c[r].x & CHEM_STATE_MASK) + (c[r].y & CHEM_STATE_MASK) + (c[r].z & CHEM_STATE_MASK) +
+                     (c[r].w & CHEM_STATE_MASK);
+  }
 }
 // transport.wgsl:71-87
 template <class S>
@@ -828,10 +851,10 @@ void launch_slope(const Dev& d, float upc, cudaStream_t s) {
   RB_LAUNCH("compute_gamma_slope", 12.0 * gc(d), s, k_slope<<<grid, dim3(BX, BY), 0, s>>>(d, upc));
 }
 void launch_thermal(const Target& t, cudaStream_t s) {
-  RB_PASS("thermal_activation", 4.0 * t.fcells, s, t, GEO_ENV, dim3(BX, BY), 0, k_thermal, nullptr);
+  RB_PASS("thermal_activation", 4.0 * t.fcells, s, t, GEO_ENV_TALL, dim3(BX, BY), 0, k_thermal, nullptr);
 }
 void launch_agg(const Target& t, cudaStream_t s) {
-  RB_PASS("agg_count", 20.0 * t.cells, s, t, GEO_ENV_LINEAR, dim3(LINEAR_THREADS), 0, k_agg_count, nullptr);
+  RB_PASS("agg_count", 20.0 * t.cells, s, t, GEO_ENV_LINEAR4, dim3(LINEAR_THREADS), 0, k_agg_count, nullptr);
   RB_PASS("agg_neighbours", 8.0 * t.cells, s, t, GEO_ENV, dim3(BX, BY), 0, k_agg_neighbours, nullptr);
 }
 void launch_scatter(const Target& t, bool simple, cudaStream_t s) {
