@@ -808,8 +808,7 @@ __global__ void __launch_bounds__(LINEAR_THREADS) k_ledger(const __grid_constant
   uint32_t a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const uint4* c4 = reinterpret_cast<const uint4*>(d.chem);
   const size_t stride = (size_t)cta.nbx * LINEAR_THREADS;
-  for (size_t i = (size_t)cta.bx * LINEAR_THREADS + threadIdx.x; i < cells; i += stride) {
-    uint4 c = __ldg(c4 + i);
+  auto add = [&](uint4 c) {
     a[0] += c.x & 0xFFFFu;
     a[1] += c.y & 0xFFFFu;
     a[2] += c.z & 0xFFFFu;
@@ -818,7 +817,18 @@ __global__ void __launch_bounds__(LINEAR_THREADS) k_ledger(const __grid_constant
     a[5] += c.y >> 16;
     a[6] += c.z >> 16;
     a[7] += c.w >> 16;
+  };
+  // four strides per round, their loads in flight together (u32 sums: the
+  // order of the adds does not change them)
+  size_t i = (size_t)cta.bx * LINEAR_THREADS + threadIdx.x;
+  for (; i + 3 * stride < cells; i += 4 * stride) {
+    const uint4 c0 = __ldg(c4 + i), c1 = __ldg(c4 + i + stride), c2 = __ldg(c4 + i + 2 * stride), c3 = __ldg(c4 + i + 3 * stride);
+    add(c0);
+    add(c1);
+    add(c2);
+    add(c3);
   }
+  for (; i < cells; i += stride) add(__ldg(c4 + i));
   __shared__ uint32_t red[LINEAR_THREADS / 32][8];
 #pragma unroll
   for (int k = 0; k < 8; k++) {
