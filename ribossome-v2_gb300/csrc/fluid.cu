@@ -299,23 +299,30 @@ __global__ void k_advect(const __grid_constant__ S s, int dir) {
 }
 
 // fluid.wgsl:479-518
-__device__ __forceinline__ float curl_at(const Dev& d, const float2* vin, uint32_t x, uint32_t y) {
-  uint32_t xm = iclamp((int)x - 1, 0, d.fw - 1), xp = iclamp((int)x + 1, 0, d.fw - 1);
-  uint32_t ym = iclamp((int)y - 1, 0, d.fh - 1), yp = iclamp((int)y + 1, 0, d.fh - 1);
-  float2 v_l = reflect_if_into_solid(d, xm, y, raw_velocity_cell(d, vin, xm, y));
-  float2 v_r = reflect_if_into_solid(d, xp, y, raw_velocity_cell(d, vin, xp, y));
-  float2 v_b = reflect_if_into_solid(d, x, ym, raw_velocity_cell(d, vin, x, ym));
-  float2 v_t = reflect_if_into_solid(d, x, yp, raw_velocity_cell(d, vin, x, yp));
-  return 0.5f * (v_r.y - v_l.y) - 0.5f * (v_t.x - v_b.x);
-}
-// curl_at for every fluid cell (input of the confinement pass).
+// curl_at for every fluid cell (input of the confinement pass).  Each
+// neighbour term reflect_if_into_solid(raw_velocity_cell(n)) is a function
+// of the neighbour alone: the CTA computes it once for its tile and the
+// 1-cell ring (coordinates clamped to the grid as curl_at clamps them, so a
+// clamped neighbour is the cell itself) and reads the four terms from there.
 template <class S>
 __global__ void k_curl(const __grid_constant__ S s, int dir) {
   RB_WORLD(s);
   const float2* __restrict__ vin = dir ? d.vb : d.va;
-  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
+  __shared__ float2 u[BY + 2][BX + 2];
+  const int x0 = cta.bx * BX, y0 = cta.by * BY, tid = threadIdx.y * BX + threadIdx.x;
+  for (int i = tid; i < (BX + 2) * (BY + 2); i += BX * BY) {
+    const int tx = i % (BX + 2), ty = i / (BX + 2);
+    const size_t n = (size_t)iclamp(y0 + ty - 1, 0, d.fh - 1) * d.fw + iclamp(x0 + tx - 1, 0, d.fw - 1);
+    const uint8_t m = __ldg(d.mask + n);
+    const float2 v = __ldg(vin + n), wn = __ldg(d.normal + n);
+    u[ty][tx] = reflect_stored(wn, m ? f2(0.0f, 0.0f) : sanitize(v));
+  }
+  __syncthreads();
+  const uint32_t x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
-  d.curl[(size_t)y * d.fw + x] = curl_at(d, vin, x, y);
+  const int tx = threadIdx.x + 1, ty = threadIdx.y + 1;
+  const float2 v_l = u[ty][tx - 1], v_r = u[ty][tx + 1], v_b = u[ty - 1][tx], v_t = u[ty + 1][tx];
+  d.curl[(size_t)y * d.fw + x] = 0.5f * (v_r.y - v_l.y) - 0.5f * (v_t.x - v_b.x);
 }
 template <class S>
 __global__ void k_vorticity(const __grid_constant__ S s, int dir) {
