@@ -23,6 +23,9 @@ CASES = [
      dict(rubble_frac=0.4, monomer_mean=12.0)),
     ("jacobi-fall-every-step", 64, None, dict(ACTIVE, sediment_settle=1.0, dt=2.0),
      dict(fluid_substep=1, terrain_mode=1, multigrid=0, jacobi_iters=8), 8, dict(rubble_frac=0.5, dt=2.0)),
+    # sides that are not multiples of the 32-cell warp rows or of the 3 x 3 classes
+    ("ragged-100x74-half-fluid", (100, 74), (50, 37), dict(ACTIVE, sediment_settle=1.0), dict(fluid_substep=1, terrain_mode=1),
+     8, dict(rubble_frac=0.35)),
 ]
 
 FIELDS = STATE_FIELDS
@@ -73,6 +76,7 @@ def test_paint_then_terrain_steps(rw, ro):
     for w in (g, o):
         w.settings.terrain_mode = 1
         w.encode_paint(20.5, 30.0, 6.5, 2)
+        w.encode_paint(0.0, 95.0, 5.0, 4)  # a disc cut by the world's corner
     g.encode_steps(4)
     o.encode_steps(4)
     compare_worlds(g, o, "terrain steps after the brush", FIELDS)
