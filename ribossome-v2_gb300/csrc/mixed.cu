@@ -139,6 +139,17 @@ __device__ __forceinline__ Cell cell_at(const MpArgs& a, int k) {
 }
 // position of cell k of this thread inside the block's region (row-major)
 __device__ __forceinline__ int cell_pos(int k) { return ((k * BY + (int)threadIdx.y) * BX) + (int)threadIdx.x; }
+// Cell k's index without its flag (0 outside the grid, a valid address):
+// the vector kernels below load a group of RG cells' inputs before they
+// compute or store any, since their stores would otherwise order every
+// later load behind them (the buffers do not alias, but are not declared so).
+constexpr int RG = 4;
+static_assert(RR % RG == 0, "cells split into whole groups");
+__device__ __forceinline__ size_t cell_idx(const MpArgs& a, int k, bool& in) {
+  const int x = blockIdx.x * BX + threadIdx.x, y = (blockIdx.y * RR + k) * BY + threadIdx.y;
+  in = x < a.fw && y < a.fh;
+  return in ? (size_t)y * a.fw + x : 0;
+}
 
 // Block sums of two values written to the per-block partials; returns true in
 // every thread of the block that finished last (its partials are visible).
@@ -397,15 +408,34 @@ __global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphCondition
 __global__ void __launch_bounds__(NT) k_mp_dots(MpArgs a) {
   float zr = 0.0f, zq = 0.0f;
 #pragma unroll
-  for (int k = 0; k < RR; k++) {
-    const Cell c = cell_at(a, k);
-    if (c.water) {
-      const float zc = a.z[c.i] - a.comp_shift[a.label[c.i]];
-      a.z[c.i] = zc;
-      zr += zc * a.r[c.i];
-      zq += zc * a.q[c.i];
-    } else if (c.in) {
-      a.z[c.i] = 0.0f;
+  for (int g = 0; g < RR; g += RG) {
+    bool in[RG];
+    uint8_t wf[RG];
+    float zv[RG], rv[RG], qv[RG], sh[RG];
+    int lb[RG];
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      const size_t i = cell_idx(a, g + k, in[k]);
+      wf[k] = in[k] ? a.fl[i] : 0;
+      zv[k] = a.z[i];
+      rv[k] = a.r[i];
+      qv[k] = a.q[i];
+      lb[k] = a.label[i];
+    }
+#pragma unroll
+    for (int k = 0; k < RG; k++) sh[k] = wf[k] ? a.comp_shift[lb[k]] : 0.0f;
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      bool inb;
+      const size_t i = cell_idx(a, g + k, inb);
+      if (wf[k]) {
+        const float zc = zv[k] - sh[k];
+        a.z[i] = zc;
+        zr += zc * rv[k];
+        zq += zc * qv[k];
+      } else if (in[k]) {
+        a.z[i] = 0.0f;
+      }
     }
   }
   if (!block_partials(a, zr, zq)) return;
@@ -438,9 +468,23 @@ __global__ void __launch_bounds__(NT) k_mp_direction(MpArgs a) {
   const float beta = a.ctl->beta;
   const bool first = a.ctl->inner == 0;  // d starts as z (whatever d held before)
 #pragma unroll
-  for (int k = 0; k < RR; k++) {
-    const Cell c = cell_at(a, k);
-    if (c.in) a.d[c.i] = c.water ? (first ? a.z[c.i] : a.z[c.i] + beta * a.d[c.i]) : 0.0f;
+  for (int g = 0; g < RR; g += RG) {
+    bool in[RG];
+    uint8_t wf[RG];
+    float zv[RG], dv[RG];
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      const size_t i = cell_idx(a, g + k, in[k]);
+      wf[k] = in[k] ? a.fl[i] : 0;
+      zv[k] = a.z[i];
+      dv[k] = a.d[i];
+    }
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      bool inb;
+      const size_t i = cell_idx(a, g + k, inb);
+      if (in[k]) a.d[i] = wf[k] ? (first ? zv[k] : zv[k] + beta * dv[k]) : 0.0f;
+    }
   }
 }
 
@@ -448,21 +492,44 @@ __global__ void __launch_bounds__(NT) k_mp_direction(MpArgs a) {
 // exactly), and d.q; alpha = z.r / d.q.
 __global__ void __launch_bounds__(NT) k_mp_matvec(MpArgs a) {
   float dq = 0.0f;
+  const int x = blockIdx.x * BX + threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < RR; k++) {
-    const Cell c = cell_at(a, k);
-    if (c.water) {
-      const float di = a.d[c.i];
-      float s = 0.0f;
-      if (c.x > 0 && a.fl[c.i - 1]) s += a.d[c.i - 1] - di;
-      if (c.x + 1 < a.fw && a.fl[c.i + 1]) s += a.d[c.i + 1] - di;
-      if (c.y > 0 && a.fl[c.i - a.fw]) s += a.d[c.i - a.fw] - di;
-      if (c.y + 1 < a.fh && a.fl[c.i + a.fw]) s += a.d[c.i + a.fw] - di;
-      const float q = s - a.eps0 * di;
-      a.q[c.i] = q;
-      dq += di * q;
-    } else if (c.in) {
-      a.q[c.i] = 0.0f;
+  for (int g = 0; g < RR; g += RG) {
+    bool in[RG];
+    uint8_t wf[RG], fn[RG][4];
+    float dc[RG], dn[RG][4];
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      const size_t i = cell_idx(a, g + k, in[k]);
+      const int y = (blockIdx.y * RR + g + k) * BY + threadIdx.y;
+      // left, right, below, above (clamped to the cell itself off the grid)
+      const size_t nb[4] = {x > 0 ? i - 1 : i, x + 1 < a.fw ? i + 1 : i, y > 0 ? i - a.fw : i, y + 1 < a.fh ? i + a.fw : i};
+      wf[k] = in[k] ? a.fl[i] : 0;
+      dc[k] = a.d[i];
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        fn[k][n] = a.fl[nb[n]];
+        dn[k][n] = a.d[nb[n]];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      bool inb;
+      const size_t i = cell_idx(a, g + k, inb);
+      const int y = (blockIdx.y * RR + g + k) * BY + threadIdx.y;
+      if (wf[k]) {
+        const float di = dc[k];
+        float sum = 0.0f;
+        if (x > 0 && fn[k][0]) sum += dn[k][0] - di;
+        if (x + 1 < a.fw && fn[k][1]) sum += dn[k][1] - di;
+        if (y > 0 && fn[k][2]) sum += dn[k][2] - di;
+        if (y + 1 < a.fh && fn[k][3]) sum += dn[k][3] - di;
+        const float q = sum - a.eps0 * di;
+        a.q[i] = q;
+        dq += di * q;
+      } else if (in[k]) {
+        a.q[i] = 0.0f;
+      }
     }
   }
   if (!block_partials(a, dq, 0.0f)) return;
@@ -484,17 +551,35 @@ __global__ void __launch_bounds__(NT) k_mp_axpy(MpArgs a, cudaGraphConditionalHa
   float rn2 = 0.0f;
   int key = 0x7fffffff;
 #pragma unroll
-  for (int k = 0; k < RR; k++) {
-    const Cell c = cell_at(a, k);
-    rn[k] = 0.0f;
-    lab[k] = -1;
-    if (c.water) {
-      a.e[c.i] += alpha * a.d[c.i];
-      rn[k] = a.r[c.i] - alpha * a.q[c.i];
-      a.r[c.i] = rn[k];
-      rn2 += rn[k] * rn[k];
-      lab[k] = a.label[c.i];
-      if (key == 0x7fffffff) key = (cell_pos(k) << 16) | lab[k];
+  for (int g = 0; g < RR; g += RG) {
+    uint8_t wf[RG];
+    float ev[RG], dv[RG], rv[RG], qv[RG];
+    int lb[RG];
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      bool in;
+      const size_t i = cell_idx(a, g + k, in);
+      wf[k] = in ? a.fl[i] : 0;
+      ev[k] = a.e[i];
+      dv[k] = a.d[i];
+      rv[k] = a.r[i];
+      qv[k] = a.q[i];
+      lb[k] = a.label[i];
+    }
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      bool in;
+      const size_t i = cell_idx(a, g + k, in);
+      rn[g + k] = 0.0f;
+      lab[g + k] = -1;
+      if (wf[k]) {
+        a.e[i] = ev[k] + alpha * dv[k];
+        rn[g + k] = rv[k] - alpha * qv[k];
+        a.r[i] = rn[g + k];
+        rn2 += rn[g + k] * rn[g + k];
+        lab[g + k] = lb[k];
+        if (key == 0x7fffffff) key = (cell_pos(g + k) << 16) | lb[k];
+      }
     }
   }
   comp_record(a, a.comp_sum_r, block_dom(key), rn, lab);
