@@ -336,35 +336,62 @@ __global__ void __launch_bounds__(NT) k_mp_residual(MpArgs a, cudaGraphCondition
   int lab[RR];
   float rn2 = 0.0f, bn2 = 0.0f;
   int key = 0x7fffffff;
+  const int x = blockIdx.x * BX + threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < RR; k++) {
-    const Cell c = cell_at(a, k);
-    rf[k] = 0.0f;
-    lab[k] = -1;
-    if (c.water) {
-      const df32 pi = df32{a.hi[c.i], a.lo[c.i]};
-      df32 s = df32{0.0f, 0.0f};
-      const int nb[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+  for (int g = 0; g < RR; g += RG) {
+    bool in[RG], inn[RG][4];
+    uint8_t wf[RG], fn[RG][4];
+    float phi[RG], plo[RG], nhi[RG][4], nlo[RG][4], bv[RG];
+    int lb[RG];
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      const size_t i = cell_idx(a, g + k, in[k]);
+      const int y = (blockIdx.y * RR + g + k) * BY + threadIdx.y;
+      // left, right, below, above (multigrid.wgsl:34-45 order), clamped to the cell off the grid
+      inn[k][0] = x > 0;
+      inn[k][1] = x + 1 < a.fw;
+      inn[k][2] = y > 0;
+      inn[k][3] = y + 1 < a.fh;
+      const size_t nb[4] = {inn[k][0] ? i - 1 : i, inn[k][1] ? i + 1 : i, inn[k][2] ? i - a.fw : i, inn[k][3] ? i + a.fw : i};
+      wf[k] = in[k] ? a.fl[i] : 0;
+      phi[k] = a.hi[i];
+      plo[k] = a.lo[i];
+      bv[k] = a.rhs[i];
+      lb[k] = a.label[i];
 #pragma unroll
       for (int n = 0; n < 4; n++) {
-        const int x = c.x + nb[n][0], y = c.y + nb[n][1];
-        if (x < 0 || y < 0 || x >= a.fw || y >= a.fh) continue;
-        const size_t j = (size_t)y * a.fw + x;
-        if (!a.fl[j]) continue;
-        s = df_add(s, df_add(df32{a.hi[j], a.lo[j]}, df_neg(pi)));
+        fn[k][n] = a.fl[nb[n]];
+        nhi[k][n] = a.hi[nb[n]];
+        nlo[k][n] = a.lo[nb[n]];
       }
-      const df32 lp = df_add(s, df_neg(df_mul_f(pi, a.eps0)));
-      const float b = a.rhs[c.i];
-      const df32 res = df_add(df32{b, 0.0f}, df_neg(lp));
-      rf[k] = res.hi + res.lo;
-      rn2 += rf[k] * rf[k];
-      bn2 += b * b;
-      lab[k] = a.label[c.i];
-      if (key == 0x7fffffff) key = (cell_pos(k) << 16) | lab[k];
     }
-    if (c.in) {
-      a.r[c.i] = rf[k];
-      a.e[c.i] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < RG; k++) {
+      bool inb;
+      const size_t i = cell_idx(a, g + k, inb);
+      rf[g + k] = 0.0f;
+      lab[g + k] = -1;
+      if (wf[k]) {
+        const df32 pi = df32{phi[k], plo[k]};
+        df32 sum = df32{0.0f, 0.0f};
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+          if (!inn[k][n] || !fn[k][n]) continue;
+          sum = df_add(sum, df_add(df32{nhi[k][n], nlo[k][n]}, df_neg(pi)));
+        }
+        const df32 lp = df_add(sum, df_neg(df_mul_f(pi, a.eps0)));
+        const float b = bv[k];
+        const df32 res = df_add(df32{b, 0.0f}, df_neg(lp));
+        rf[g + k] = res.hi + res.lo;
+        rn2 += rf[g + k] * rf[g + k];
+        bn2 += b * b;
+        lab[g + k] = lb[k];
+        if (key == 0x7fffffff) key = (cell_pos(g + k) << 16) | lab[g + k];
+      }
+      if (in[k]) {
+        a.r[i] = rf[g + k];
+        a.e[i] = 0.0f;
+      }
     }
   }
   if (!final_pass) comp_record(a, a.comp_sum_r, block_dom(key), rf, lab);
