@@ -1,7 +1,7 @@
 """FP64 reference solve of the world step's pressure problem.
 
-Test infrastructure: the tests and the benchmark's accuracy check call it
-to check the mixed-precision pressure solve; the library never does.
+Test infrastructure: the tests call it to check the mixed-precision
+pressure solve; the library and the benchmark never do.
 
 The operator is the level-0 operator of the reference's multigrid
 (shaders/world/multigrid.wgsl:29-77: the Gauss-Seidel update
