@@ -58,3 +58,25 @@ def test_fp64_solution_is_a_fixed_point_of_the_reference_multigrid(ro, rw):
     o.run_pass(o.params, 8)
     far = o.read(rw.PRESSURE).astype(np.float64)
     assert np.linalg.norm(np.where(water, far - want, 0)) / np.linalg.norm(want) > 1e-2
+
+
+def test_benchmark_residual_matches_the_fp64_oracle():
+    """bench.py re-checks the mixed-precision solve with its own FP64 residual
+    (it may not call the oracle); both evaluate ||rhs - L p|| / ||rhs|| with the
+    same level-0 operator."""
+    import os
+    import sys
+
+    import numpy as np
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    import fp64_pressure as fp
+
+    rng = np.random.default_rng(5)
+    for shape in ((33, 47), (64, 64)):
+        water = rng.random(shape) > 0.15
+        p = rng.standard_normal(shape) * 3.0
+        b = rng.standard_normal(shape)
+        assert bench.host_rel_residual(p, b, water) == fp.rel_residual(p, b, water)
