@@ -63,7 +63,8 @@ void geo_blocks(Geo g, const Dev& d, int* nbx, int* nby) {
       return;
     case GEO_LEDGER: {
       long long b = (cells + LEDGER_CELLS_PER_CTA - 1) / LEDGER_CELLS_PER_CTA;
-      *nbx = (int)(b < 1 ? 1 : (b > 152 * 8 ? 152 * 8 : b));
+      const long long cap = 8ll * device_sm_count();  // eight CTAs per SM stream the whole grid
+      *nbx = (int)(b < 1 ? 1 : (b > cap ? cap : b));
       *nby = 1;
       return;
     }

@@ -597,13 +597,12 @@ void launch_subtract_gradient(const Target& t, int dir, cudaStream_t s) {
   RB_PASS("subtract_gradient", 21.0 * t.fcells, s, t, GEO_FLUID, dim3(BX, BY), 0, k_subtract_gradient, nullptr, dir);
 }
 void launch_net_flux(const Target& t, int dir, cudaStream_t s) {
-  static uint64_t attr_done = 0;  // one bit per device: the double buffer is above the 48 KB default
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (!(attr_done >> (dev & 63) & 1ull)) {
+  static DeviceOnce attr;  // the double buffer is above the 48 KB default
+  const int dev = DeviceOnce::device();
+  if (attr.pending(dev)) {
     cudaFuncSetAttribute(k_net_flux<OneWorld>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NF_SMEM);
     cudaFuncSetAttribute(k_net_flux<WorldSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NF_SMEM);
-    attr_done |= 1ull << (dev & 63);
+    attr.done(dev);
   }
   RB_PASS("net_flux", 18.0 * t.fcells, s, t, GEO_NET_FLUX, dim3(NF_THREADS), NF_SMEM, k_net_flux, nullptr, dir);
 }

@@ -707,13 +707,13 @@ static const char* const POST_NAMES[8] = {"mg_prolong_post_L0", "mg_prolong_post
                                           "mg_prolong_post_L6", "mg_prolong_post_L7+"};
 
 // Box of a fine level: the 66 x 50 box where it gives at least three tiles
-// per SM (152 SMs), the 34 x 34 box on the smaller levels, whose kernels are
+// per SM of the device, the 34 x 34 box on the smaller levels, whose kernels are
 // bound by the latency of one tile rather than by bandwidth (measured on the
 // 2048^2 levels: 1024^2 is faster with the big box, 512^2 with the small).
 static bool small_tiles(const MgLevel& L, const MgConfig& c) {
   const int H = 2 * c.pre + 1, tw = BoxBig::tile_w(H), th = BoxBig::tile_h(H);
   const long big = (long)((L.nx + tw - 1) / tw) * ((L.ny + th - 1) / th);
-  return big < 3 * 152;
+  return big < 3l * device_sm_count();
 }
 
 // Tiles of a fine level's pre (halo 2 pre + 1) or post (halo 2 post) pass.
@@ -752,15 +752,14 @@ bool multigrid_fused_ok(const MgLevel* levels, int nl, const MgConfig& c) {
 }
 
 static void set_smem_attrs() {
-  static uint64_t attr_done = 0;  // one bit per device
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (attr_done >> (dev & 63) & 1ull) return;
+  static DeviceOnce attr;
+  const int dev = DeviceOnce::device();
+  if (!attr.pending(dev)) return;
   const int mx = (int)COARSE_SMEM_MAX;
   cudaFuncSetAttribute(k_mg_coarse<CoarseOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseMany>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_mg_coarse<CoarseOne, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  attr_done |= 1ull << (dev & 63);
+  attr.done(dev);
 }
 
 // The pre- and post-smooth passes of fine level l.  Level 0 reads

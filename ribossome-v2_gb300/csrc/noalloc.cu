@@ -28,9 +28,10 @@ constexpr uint64_t NOALLOC_MAX_CELLS = 512ull * 512ull;
 // at most 4/3 of the finest level plus one 64-cell pad per level.
 constexpr uint64_t NOALLOC_MAX_LEVEL_CELLS = NOALLOC_MAX_CELLS * 4 / 3 + 64 * 16;
 // p, rhs, p2 (floats, all levels) + p_tmp (floats, level 0) + water flags
-// (bytes, all levels) + wall mask (bytes, level 0) + status word.
+// (bytes, all levels) + wall mask (bytes, level 0), plus 256-byte alignment
+// of each of the six blocks.
 constexpr uint64_t NOALLOC_SCRATCH_BYTES =
-    3 * 4 * NOALLOC_MAX_LEVEL_CELLS + 4 * NOALLOC_MAX_CELLS + NOALLOC_MAX_LEVEL_CELLS + NOALLOC_MAX_CELLS + 256 * 8;
+    3 * 4 * NOALLOC_MAX_LEVEL_CELLS + 4 * NOALLOC_MAX_CELLS + NOALLOC_MAX_LEVEL_CELLS + NOALLOC_MAX_CELLS + 256 * 6;
 
 // ~6.2 MB per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
@@ -126,7 +127,6 @@ extern "C" ribo_status ribo_pressure_solve_noalloc(uint32_t fluid_w, uint32_t fl
   b.p_tmp = reinterpret_cast<float*>(take(cells * 4));
   b.fluid = take(off);
   uint8_t* mask = take(cells);
-  uint32_t* status = reinterpret_cast<uint32_t*>(take(4));
   if (at > NOALLOC_SCRATCH_BYTES) return set_error(RIBO_INVALID_ARG, "scratch layout overflow");
 
   Dev d{};
@@ -137,12 +137,10 @@ extern "C" ribo_status ribo_pressure_solve_noalloc(uint32_t fluid_w, uint32_t fl
   d.div = const_cast<float*>(d_divergence);
   d.pa = d_pressure;
   d.fluid0 = b.fluid + levels[0].off;
-  d.status = status;
-
-  // The status word must start at zero; everything else is written before
-  // it is read within the call.
-  st = cuda_status(cudaMemsetAsync(status, 0, 4, stream), "status");
-  if (st != RIBO_OK) return st;
+  // No kernel of the solve waits on anything or reports through a status
+  // word, so none is passed.  Every scratch word the solve reads is written
+  // earlier in the same call, so nothing needs clearing between calls.
+  d.status = nullptr;
   k_noalloc_flags<<<(unsigned)((cells + 255) / 256), 256, 0, stream>>>(d_solid_mask, mask, d.fluid0, cells);
   launch_multigrid_fused(d, levels, nl, b, c, stream);
   return cuda_status(cudaGetLastError(), "noalloc pressure solve");

@@ -5,9 +5,43 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "ribo_dev.cuh"
 
 namespace ribo {
+
+// Per-device one-time set-up (kernel attributes and the like) that may be
+// reached from several host threads: `pending()` says whether the current
+// device still needs it, `done()` records it.  Two threads that race both
+// run the set-up, which is idempotent; no bit is ever lost.
+struct DeviceOnce {
+  std::atomic<uint64_t> bits{0};
+  static int device() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev & 63;
+  }
+  bool pending(int dev) const { return !((bits.load(std::memory_order_acquire) >> dev) & 1ull); }
+  void done(int dev) { bits.fetch_or(1ull << dev, std::memory_order_release); }
+};
+
+// Streaming multiprocessors of the current device, queried once per device
+// (grid sizes and tile choices scale with it).  Without an answering device
+// (a host-only size computation) it is the GB300's 152.
+inline int device_sm_count() {
+  static std::atomic<int> cache[64];
+  const int dev = DeviceOnce::device();
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      return 152;
+    }
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 // Per-launch instrumentation: every kernel launch of the library goes
 // through RB_LAUNCH, which counts it and, when kernel timing is enabled on

@@ -873,13 +873,12 @@ void launch_scatter(const Target& t, bool simple, cudaStream_t s) {
     RB_PASS("transport_scatter_simple", bytes, s, t, GEO_ENV, dim3(BX, BY), 0, k_scatter, nullptr);
     return;
   }
-  static uint64_t attr_done = 0;  // one bit per device
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (!(attr_done >> (dev & 63) & 1ull)) {
+  static DeviceOnce attr;
+  const int dev = DeviceOnce::device();
+  if (attr.pending(dev)) {
     cudaFuncSetAttribute(k_scatter_tiled<OneWorld>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(st::Smem));
     cudaFuncSetAttribute(k_scatter_tiled<WorldSet>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(st::Smem));
-    attr_done |= 1ull << (dev & 63);
+    attr.done(dev);
   }
   RB_PASS("transport_scatter", bytes, s, t, GEO_SCATTER, dim3(st::NT), sizeof(st::Smem), k_scatter_tiled, nullptr);
 }

@@ -207,15 +207,15 @@ ribo_status World::alloc(void** p, size_t bytes, const char* what) {
 }
 
 static void keep_pool_memory(int dev) {
-  static uint64_t done = 0;  // one bit per device
-  if (done >> (dev & 63) & 1ull) return;
+  static DeviceOnce once;
+  if (!once.pending(dev & 63)) return;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
     uint64_t keep = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   cudaGetLastError();
-  done |= 1ull << (dev & 63);
+  once.done(dev & 63);
 }
 
 // Multigrid levels (src/world/mod.rs:637-671): halve while both sides are

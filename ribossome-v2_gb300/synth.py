@@ -119,10 +119,14 @@ def make_world_inputs(grid, fluid=None, seed: int = 1000, rock_frac: float = 0.1
     }
 
 
-def bench_params(seed: int = 1000) -> "rw.SimParams":
+def bench_params(seed: int = 1000, defaults=None) -> "rw.SimParams":
     """SimParams of the benchmark workload: reference defaults, dt = 1,
-    sun heating off, every step a full fluid + transport step."""
-    p = rw.default_params(seed)
+    sun heating off, every step a full fluid + transport step.
+
+    `defaults(seed)` supplies the reference defaults; the library's own
+    table by default.  A caller that must not load the CUDA library (a
+    CPU-only measurement) passes a table of its own."""
+    p = (defaults or rw.default_params)(seed)
     p.dt = 1.0
     p.sun_heat = 0.0
     p.transport_every = 1

@@ -149,3 +149,21 @@ def test_server_bad_arguments(rw):
     assert lib.ribo_server_submit(None, None, None) == 1
     assert lib.ribo_server_iterate(None, None) == 1
     lib.ribo_server_destroy(None)
+
+
+def test_reference_arm_runs_without_the_cuda_library(ro):
+    """bench.py --impl reference times the CPU restatement alone: its process
+    maps the oracle's library and never the product's (its SimParams come
+    from the oracle's own table of the reference defaults)."""
+    import json
+    import sys
+
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--size", "64",
+                          "--steps", "3", "--warmup", "3", "--reference-seconds", "1"],
+                         capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    libs = line["native_libraries"]
+    assert any("libribo_oracle" in p for p in libs), libs
+    assert not any("libribo_world" in p for p in libs), libs

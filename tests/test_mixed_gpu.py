@@ -102,3 +102,16 @@ def test_mixed_mode_rejections(rw):
         f.read(rw.PRESSURE_LO)
     f.close()
     w.close()
+
+
+def test_full_size_solves_reach_tolerance(rw):
+    """The mixed-precision configuration at the benchmark's size (2048^2,
+    FP16-storage levels 0-3, FP32 defect correction, FP64 coarsest solve and
+    mean removal): each of two steps' solves reaches a relative residual of
+    1e-5 against the FP64 operator, evaluated on the host in FP64 from the
+    pressure pair the GPU left."""
+    w = mixed_world(rw, 2048, seed=1000)
+    for call in range(2):
+        w.encode_steps(1)
+        check_solve(rw, w, f"2048^2 step {call + 1}")
+    w.close()

@@ -213,3 +213,44 @@ def test_async_ledger_readback(rw):
     w.request_ledger()
     w.sync()
     assert w.poll_ledger() == w.ledger_blocking()
+
+
+def _bench_pair(rw, ro, n, seed=1000):
+    """A GPU world and an oracle world with the benchmark's settings: F = G,
+    multigrid to 16x16, 4 V-cycles of 3+3 sweeps, 30 coarse sweeps, fluid and
+    transport every step, dt = 1, sun heating off, reference defaults (the
+    oracle's own table on its side)."""
+    import synth
+
+    g = rw.World(n, seed=seed, mg_min_size=16, mg_pre=3, mg_post=3)
+    o = ro.OracleWorld(n, seed=seed, mg_min_size=16, mg_pre=3, mg_post=3)
+    inputs = synth.make_world_inputs(n, seed=seed)
+    g.seed_inputs(inputs)
+    o.seed_inputs(inputs)
+    g.params = synth.bench_params(seed)
+    o.params = synth.bench_params(seed, defaults=ro.default_params)
+    assert bytes(g.params) == bytes(o.params), "the library's default table differs from the oracle's"
+    for w in (g, o):
+        w.settings.fluid_substep = 1
+        w.settings.mg_cycles = 4
+    return g, o
+
+
+@pytest.mark.parametrize("n,steps", [(2048, 2), (1024, 3)], ids=["2048-bench-config", "1024-big-box-multigrid"])
+def test_benchmark_configuration_bit_exact(rw, ro, n, steps):
+    """The configuration the benchmark times, stepped on the GPU and on the
+    oracle, every field compared bit for bit after each step.  At 2048^2 and
+    1024^2 the two finest multigrid levels run the 66 x 50 box kernels (the
+    level picks them once it has three tiles per SM), which smaller parity
+    cases never reach; 2048^2 is the benchmark's own size and schedule
+    (src/world/mod.rs:1545-1577 with MG_PRE = MG_POST = 3, 4 cycles, 8
+    levels)."""
+    g, o = _bench_pair(rw, ro, n)
+    compare_worlds(g, o, f"{n}^2 after upload")
+    for s in range(steps):
+        g.encode_steps(1)
+        o.encode_steps(1)
+        compare_worlds(g, o, f"{n}^2 after {s + 1} steps")
+    assert g.ledger_blocking() == o.ledger_blocking()
+    g.close()
+    o.close()

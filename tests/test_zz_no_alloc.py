@@ -26,15 +26,24 @@ def _entry(rw):
     return lib, fn
 
 
-def test_noalloc_pressure_solve_matches_world_step(rw):
+# (fluid width, height): the square the limit allows, a level-0 grid small
+# enough for the single-CTA coarse kernel to take whole (it then reads the
+# caller's wall mask, divergence and pressure directly), a rectangle, a grid
+# whose halving stops early at odd sides (90 x 66 -> 45 x 33), and the
+# largest grid the scratch holds.
+GRIDS = [(256, 256), (64, 64), (96, 160), (90, 66), (512, 512)]
+
+
+@pytest.mark.parametrize("grid", GRIDS, ids=[f"{w}x{h}" for w, h in GRIDS])
+def test_noalloc_pressure_solve_matches_world_step(rw, grid):
     import torch
 
     import synth
 
     lib, fn = _entry(rw)
-    n = 256
-    w = rw.World(n, seed=5, mg_min_size=16, mg_pre=3, mg_post=3)
-    w.seed_inputs(synth.make_world_inputs(n, seed=5))
+    nw, nh = grid
+    w = rw.World(grid, seed=5, mg_min_size=16, mg_pre=3, mg_post=3)
+    w.seed_inputs(synth.make_world_inputs(grid, seed=5))
     w.params.dt = 1.0
     w.params.transport_every = 1
     w.params.sun_heat = 0.0
@@ -51,12 +60,13 @@ def test_noalloc_pressure_solve_matches_world_step(rw):
         t_mask = torch.from_numpy(np.ascontiguousarray(mask).view(np.int32)).cuda()
         t_p = torch.from_numpy(p0).cuda()
         torch.cuda.synchronize()
-        st = fn(n, n, t_div.data_ptr(), t_mask.data_ptr(), t_p.data_ptr(), 16, 3, 3, 30, 2, None)
+        st = fn(nw, nh, t_div.data_ptr(), t_mask.data_ptr(), t_p.data_ptr(), 16, 3, 3, 30, 2, None)
         assert st == 0, lib.ribo_last_error()
         torch.cuda.synchronize()
         got = t_p.cpu().numpy()
         diff = np.nonzero(got.view(np.uint32) != p1.view(np.uint32))[0]
-        assert diff.size == 0, f"call {call}: {diff.size} cells differ, first {diff[:3]}"
+        assert diff.size == 0, f"{nw}x{nh} call {call}: {diff.size} cells differ, first {diff[:3]}"
+    w.close()
 
 
 def test_noalloc_rejects_grids_above_the_scratch_limit(rw):
