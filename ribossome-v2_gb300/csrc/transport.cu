@@ -356,26 +356,47 @@ constexpr int TX = SCATTER_TX, TY = SCATTER_TY, NT = TX * TY;
 constexpr int HALO = 2, AW = TX + 2 * HALO, AH = TY + 2 * HALO, AC = AW * AH;
 constexpr uint16_t FAR = 0xFFFFu;  // destination outside the accumulator
 
-// Per (cell, channel) word of the mover loop: bits 0-8 the activated count
-// after the local reactions, capped at 511 (a mover index k is below
-// MAX_MOVERS_PER_CH <= 511, so k < act_n reads the same); bits 9-24 the
-// activated counts m of the four neighbours in this channel, each capped at
-// 8 (4 bits; 15 where the neighbour is off the grid), which select the
-// cohesion factor cohf[m] = 1 + cohesion * m of an activated monomer's hop
-// weights (cohf is 1 for m = 15 and wherever cohesion is off).
-constexpr uint32_t ACT_BITS = 9, ACT_MASK = (1u << ACT_BITS) - 1u;
-static_assert(MAX_MOVERS_PER_CH <= ACT_MASK, "mover index must fit the activated-count field");
+// The movers of a warp are its non-empty (cell, channel) segments in order,
+// listed with a record each: the hash head (x1) of the cell-channel slot and
+// a packed word -- bits 0-14 the segment's first mover in the warp's order,
+// 15-19 the cell's lane, 20-21 the channel, 22-30 the activated count after
+// the local reactions capped at MAX_MOVERS_PER_CH (a mover index k is below
+// it, so k < act reads the same).
+constexpr uint32_t SEG_START_BITS = 15, SEG_LANE_SHIFT = 15, SEG_CH_SHIFT = 20, SEG_ACT_SHIFT = 22;
+static_assert(TX * 4 * MAX_MOVERS_PER_CH <= (1u << SEG_START_BITS), "warp mover positions must fit the start field");
+static_assert(MAX_MOVERS_PER_CH < 512u, "the activated count must fit 9 bits");
+constexpr int NSEG = 4 * TX;            // segments of a warp at most
+constexpr int SSTART = NSEG + TX + 1;   // start table: a step looks up to 32 entries past the current one
+constexpr uint16_t NO_START = 0xFFFFu;  // past the listed segments (above every mover position)
+// Movers that hop (diffusion, squeeze) or come from a dispersing rubble cell
+// take the general path: the main loop queues them (HQ entries per warp)
+// and runs the queue densely, so the rarely taken branch is not a step of
+// the whole warp in most iterations.
+constexpr int HQ = 64;
+// The mover loop compares the top 24 bits of a draw with integer
+// thresholds: rb_u2f(z) < p exactly when (z >> 8) < ceil(p * 2^24), for p
+// in [0, 1] (rb_u2f is (z >> 8) * 2^-24, and scaling by 2^24 is exact; a NaN
+// or negative p gives 0, below every draw, as the float test is false).
+__device__ __forceinline__ uint32_t u24_threshold(float p) { return rb_f2u(ceilf(p * 16777216.0f)); }
+constexpr uint32_t ALWAYS = 1u << 24;  // a threshold every draw is below
 
 struct Smem {
   // per cell (index = warp * 32 + lane)
-  float4 mv0[NT];                  // displacement x, y; p_diff; p_diff + p_settle
-  float4 mv1[NT];                  // p_bound; bound start x, y; dispersion length (or -1)
+  float4 mv0[NT];                  // displacement x, y; bound start x, y
+  uint4 thr[NT];                   // p_bound (float bits); general-path, hop and settle thresholds
+  float dlen[NT];                  // dispersion length, or -1 where the cell does not disperse
+  int2 base[NT];                   // window origin: floor(displacement) - 1 per axis
   float4 press[NT];                // osmotic hop weights (+x, -x, +y, -y)
   float acc[8][NT];                // Kawasaki acceptance per direction: activated 0-3, spent 4-7
-  uint32_t segw[4][NT];            // per channel: activated count | neighbour counts (above)
-  uint32_t head[4][NT];            // per channel: hash head (x1) of the cell-channel slot
+  // per channel: the activated counts m of the four neighbours, 4 bits each
+  // (capped at 8; 15 off the grid), which select the cohesion factor
+  // cohf[m] = 1 + cohesion * m of an activated monomer's hop weights (cohf
+  // is 1 for m = 15 and wherever cohesion is off)
+  uint16_t nbw[4][NT];
   uint16_t slot[16][NT];           // accumulator slot of each window bin (blocking resolved), or FAR
-  uint32_t off[TY][4 * TX + 1];    // per warp: exclusive prefix of movers over (cell, channel)
+  uint2 rec[TY][NSEG];             // per warp: segment records (above)
+  uint16_t sstart[TY][SSTART];     // per warp: first mover of each listed segment, then NO_START
+  uint16_t hq[TY][HQ];             // per warp: queued general-path movers, segment << 8 | mover index
   uint32_t accum[4][AC];           // tile + ring destination sums [channel][cell] (lanes on
                                    // neighbouring cells hit neighbouring banks)
   uint8_t rock[AC];                // destination is rock
@@ -474,11 +495,37 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
 
   // ---- A. per-cell part (transport.wgsl:120-304) ----
   const uint32_t x = X0 + lane, y = Y0 + warp;
-  uint32_t mov[4] = {0u, 0u, 0u, 0u};
   const int sax = lane + st::HALO, say = warp + st::HALO;  // own accumulator cell
-  if (x < G && y < GH) {
-    const size_t idx = (size_t)y * G + x;
-    const uint4 cw = load_cell(d.chem, idx);
+  const bool in_grid = x < G && y < GH;
+  const size_t idx = (size_t)y * G + x;
+  const uint4 cw = in_grid ? load_cell(d.chem, idx) : make_uint4(0u, 0u, 0u, 0u);
+  // Movers per channel: min(act + spent, MAX_MOVERS_PER_CH), which the local
+  // reactions leave unchanged, so the warp places its segments first: the
+  // cell's first listed segment and the movers of the warp before the cell.
+  uint32_t seg_pos, mover_pos, total, nseg;
+  {
+    const uint32_t m0 = umin(word_total(cw.x), MAX_MOVERS_PER_CH), m1 = umin(word_total(cw.y), MAX_MOVERS_PER_CH);
+    const uint32_t m2 = umin(word_total(cw.z), MAX_MOVERS_PER_CH), m3 = umin(word_total(cw.w), MAX_MOVERS_PER_CH);
+    const uint32_t cell_sum = m0 + m1 + m2 + m3;
+    const uint32_t nz = (m0 > 0u ? 1u : 0u) + (m1 > 0u ? 1u : 0u) + (m2 > 0u ? 1u : 0u) + (m3 > 0u ? 1u : 0u);
+    uint32_t incl = cell_sum, incl_nz = nz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      const uint32_t tn = __shfl_up_sync(0xffffffffu, incl_nz, o);
+      if (lane >= o) {
+        incl += t;
+        incl_nz += tn;
+      }
+    }
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    nseg = __shfl_sync(0xffffffffu, incl_nz, 31);
+    seg_pos = incl_nz - nz;
+    mover_pos = incl - cell_sum;
+  }
+  // the start table past the listed segments
+  for (int i = (int)nseg + lane; i < st::SSTART; i += 32) S.sstart[warp][i] = st::NO_START;
+  if (in_grid) {
     const uint32_t src_total = cell_total4(cw);
     if (src_total != 0u) {
       const uint32_t g_src = __ldg(d.gamma + idx);
@@ -562,12 +609,16 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         float t_rel = 1.0f + rb_max(d.temp_in[(size_t)fy * d.fw + fx], 0.0f) / TEMP_ACT_THRESHOLD;
         float room = rb_clamp(5.0f * (1.0f - (float)src_total / (float)(cap_self > 1u ? cap_self : 1u)), 0.0f, 1.0f);
         float k_e = P->aggregation * room / t_rel;
+        // drop = e0 - ek and rise = ek - e0 are exact negatives of each
+        // other, so at most one is positive and it equals |e0 - ek|: one
+        // exponential per direction gives both acceptances, the same four
+        // calls on every lane instead of a divergent pair per direction.
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-          float drop = e[0] - e[k + 1];
-          if (drop > 0.0f) acc[k] = rb_exp(-k_e * drop);
-          float rise = e[k + 1] - e[0];
-          if (rise > 0.0f) accs[k] = rb_exp(-k_e * rise);
+          const float drop = e[0] - e[k + 1];
+          const float a = rb_exp(-k_e * rb_abs(drop));
+          if (drop > 0.0f) acc[k] = a;
+          else if (drop < 0.0f) accs[k] = a;
         }
         p_bound = 1.0f - rb_exp(-k_e * rb_min(rb_max(e[0] - 1.0f, 0.0f), 48.0f));
       }
@@ -583,8 +634,20 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       }
       const bool disperse = g_src > 0u && (disp.x != 0.0f || disp.y != 0.0f);
       const int basex = rb_floor_i(disp.x) - 1, basey = rb_floor_i(disp.y) - 1;
-      S.mv0[tid] = make_float4(disp.x, disp.y, p_diff, p_diff + p_settle);
-      S.mv1[tid] = make_float4(p_bound, bound_start.x, bound_start.y, disperse ? len2(disp) : -1.0f);
+      S.mv0[tid] = make_float4(disp.x, disp.y, bound_start.x, bound_start.y);
+      S.base[tid] = make_int2(basex, basey);
+      {
+        // A dispersing cell sends every mover down the general path, and so
+        // does a displacement of 2^22 cells or more.  Below that a start s
+        // in [0, 1] gives fl(s + d) in [d, d + 1] exactly at the ends, so a
+        // main-path mover's window offset is 1 or 2 per axis (0 or 1 in y
+        // after settling) and its bin needs no clamp.
+        const bool general_only = disperse || !(rb_abs(disp.x) < 4194304.0f && rb_abs(disp.y) < 4194304.0f);
+        const uint32_t t_hop = st::u24_threshold(p_diff);
+        S.thr[tid] = make_uint4(__float_as_uint(p_bound), general_only ? st::ALWAYS : t_hop, t_hop,
+                                st::u24_threshold(p_diff + p_settle));
+      }
+      S.dlen[tid] = disperse ? len2(disp) : -1.0f;
       S.press[tid] = make_float4(press[0], press[1], press[2], press[3]);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
@@ -634,11 +697,9 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         const uint32_t slot = (uint32_t)(idx * 4 + ch);
         uint32_t act_n = words[ch] & CHEM_STATE_MASK;
         uint32_t spent_n = words[ch] >> 16;
-        S.segw[ch][tid] = 0u;
         if (act_n + spent_n == 0u) continue;
         // rb_pcg4d(slot, epoch, RB_S_PHOTO / RB_S_DECAY, seed), sharing the slot's head
         const st::PcgHead rh = st::pcg_head(slot, P->epoch, P->seed);
-        S.head[ch][tid] = rh.x1;
         if (spent_n > 0u) {
           float sens = 1.0f + CHEM_SENSITIZE * (float)umin(act_n, 8u);
           float exp_act = (float)umin(spent_n, 8u) * tn * (light_term * sens + rb_max(P->reactivation_rate, 0.0f));
@@ -661,88 +722,59 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         const uint32_t act_stay = act_n - umin(act_n, movers);
         const uint32_t stay = act_stay + (n - movers - act_stay) * CHEM_SPENT_ONE;
         if (stay) atomicAdd(&S.accum[ch][say * st::AW + sax], stay);
-        S.segw[ch][tid] = umin(act_n, st::ACT_MASK) | (act_n > 0u ? nbm[ch] << st::ACT_BITS : 0u);
-        mov[ch] = movers;
+        S.nbw[ch][tid] = (uint16_t)nbm[ch];
+        S.rec[warp][seg_pos] = make_uint2(rh.x1, mover_pos | (uint32_t)lane << st::SEG_LANE_SHIFT |
+                                                     ch << st::SEG_CH_SHIFT |
+                                                     umin(act_n, MAX_MOVERS_PER_CH) << st::SEG_ACT_SHIFT);
+        S.sstart[warp][seg_pos] = (uint16_t)mover_pos;
+        seg_pos++;
+        mover_pos += movers;
       }
     }
   }
 
-  // ---- B. movers, split evenly over the lanes of the warp ----
-  uint32_t cell_sum = mov[0] + mov[1] + mov[2] + mov[3];
-  uint32_t incl = cell_sum;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-  {
-    uint32_t base = incl - cell_sum;
-    uint32_t* off = S.off[warp];
-    off[lane * 4 + 0] = base;
-    off[lane * 4 + 1] = base + mov[0];
-    off[lane * 4 + 2] = base + mov[0] + mov[1];
-    off[lane * 4 + 3] = base + mov[0] + mov[1] + mov[2];
-    if (lane == 31) off[128] = total;
-  }
+  // ---- B. movers: the warp takes 32 consecutive movers per step ----
+  // Lane l of a step takes mover jb + l of the warp's order.  Its segment is
+  // the one holding mover jb plus the segments that start in (jb, jb + l]:
+  // the lanes read the next 32 segment starts (segments are not empty, so at
+  // most 32 of them start in a window of 32 movers) and mark those inside
+  // the window.  Every lane runs the same instructions; the movers that
+  // hop or disperse are queued and run together at the end of the warp's
+  // movers, or when the queue fills.
   __syncthreads();
-
-  const uint32_t chunk = (total + 31u) / 32u;
-  uint32_t j = umin(total, lane * chunk);
-  const uint32_t j_end = umin(total, j + chunk);
-  if (j < j_end) {
-    const uint32_t* off = S.off[warp];
-    int lo = 0, hi = 127;  // segment s with off[s] <= j < off[s+1] (the largest such s)
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (off[mid] <= j) lo = mid;
-      else hi = mid - 1;
-    }
-    int s = lo;
-    uint32_t k = j - off[s];
-    uint32_t seg_end = off[s + 1];
-    int c = s >> 2, ch = s & 3;
-    int ct = warp * 32 + c;
+  {
+    const uint2* rec = S.rec[warp];
+    const uint16_t* sstart = S.sstart[warp];
+    uint16_t* hq = S.hq[warp];
+    const st::PcgHead ph0 = st::pcg_head(0u, P->epoch, P->seed);  // y0, w0 of every move draw of the step
     const int cy = Y0 + warp;
-    int cx = X0 + c;
-    const uint32_t epoch = P->epoch, seed = P->seed;
-    // per segment: the hash head of its slot, the cell's mover parameters
-    // the slot's hash head, left by the per-cell part (y0, w0 are the step's)
-    st::PcgHead ph = st::pcg_head(0u, epoch, seed);
-    ph.x1 = S.head[ch][ct];
-    uint32_t segw = S.segw[ch][ct];
-    float4 mv0 = S.mv0[ct], mv1 = S.mv1[ct];
-    int basex = rb_floor_i(mv0.x) - 1, basey = rb_floor_i(mv0.y) - 1;
-    // z word of the move draw for mover k (stepped with k below)
-    uint32_t zk = st::pcg_z0(RB_S_MOVE + k);
+    const uint32_t lt_mask = (1u << lane) - 1u, le_mask = 0xFFFFFFFFu >> (31 - lane);
     constexpr uint32_t Z_DISPERSE = st::pcg_z0(RB_S_DISPERSE) - st::pcg_z0(RB_S_MOVE);
-    for (; j < j_end; j++, k++, zk += 1664525u) {
-      if (j >= seg_end) {  // next non-empty segment; it starts at mover 0
-        do {
-          s++;
-          seg_end = off[s + 1];
-        } while (j >= seg_end);
-        k = 0u;
-        zk = st::pcg_z0(RB_S_MOVE);
-        c = s >> 2;
-        ch = s & 3;
-        ct = warp * 32 + c;
-        cx = X0 + c;
-        ph.x1 = S.head[ch][ct];
-        segw = S.segw[ch][ct];
-        mv0 = S.mv0[ct];
-        mv1 = S.mv1[ct];
-        basex = rb_floor_i(mv0.x) - 1;
-        basey = rb_floor_i(mv0.y) - 1;
-      }
-      const bool is_act = k < (segw & st::ACT_MASK);
+    constexpr uint32_t START_MASK = (1u << st::SEG_START_BITS) - 1u;
+
+    // the general path of mover k of segment s (transport.wgsl:306-406):
+    // bound or uniform start, displacement, rubble dispersion, the
+    // diffusion / squeeze hop with osmotic and cohesion weights and Kawasaki
+    // acceptance, settling; then the window bin and its accumulator slot, or
+    // a global atomic beyond the ring
+    auto general = [&](uint32_t q) {
+      const uint32_t s = q >> 8, k = q & 255u;
+      const uint2 r = rec[s];
+      const int ct = warp * 32 + (int)((r.y >> st::SEG_LANE_SHIFT) & 31u), ch = (int)((r.y >> st::SEG_CH_SHIFT) & 3u);
+      const bool is_act = k < (r.y >> st::SEG_ACT_SHIFT);
       const uint32_t unit = is_act ? 1u : CHEM_SPENT_ONE;
+      const float4 m0 = S.mv0[ct];
+      const uint4 th = S.thr[ct];
+      const float dlen = S.dlen[ct];
+      st::PcgHead ph = ph0;
+      ph.x1 = r.x;
+      const uint32_t zk = st::pcg_z0(RB_S_MOVE + k);
       const rb_u4 ru = st::pcg_draw(ph, zk);  // rb_pcg4d(slot, epoch, RB_S_MOVE + k, seed)
       const float rfx = rb_u2f(ru.x), rfy = rb_u2f(ru.y), rfz = rb_u2f(ru.z), rfw = rb_u2f(ru.w);
-      const float p_bound = mv1.x, dlen = mv1.w;
+      const float p_bound = __uint_as_float(th.x);
       const bool bound = is_act && p_bound > 0.0f && rb_fract(rfz * (float)7.31 + rfw * (float)3.17) < p_bound;
-      float px = (bound ? mv1.y : rfx) + mv0.x;
-      float py = (bound ? mv1.z : rfy) + mv0.y;
+      float px = (bound ? m0.z : rfx) + m0.x;
+      float py = (bound ? m0.w : rfy) + m0.y;
       if (dlen >= 0.0f) {
         const rb_u4 rj = st::pcg_draw(ph, zk + Z_DISPERSE);  // rb_pcg4d(slot, epoch, RB_S_DISPERSE + k, seed)
         float jxx = (rb_u2f(rj.x) * 2.0f - 1.0f) * dlen * RUBBLE_DISPERSION;
@@ -750,11 +782,12 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         px += rb_clamp(jxx, (float)-0.9, (float)0.9);
         py += rb_clamp(jyy, (float)-0.9, (float)0.9);
       }
-      if (rfz < mv0.z) {
+      const uint32_t z24 = ru.z >> 8;
+      if (z24 < th.z) {  // rfz < p_diff
         // hop weights: osmotic pressure times, for an activated monomer, the
         // cohesion factors (transport.wgsl:298-304)
         const float4 pr = S.press[ct];
-        const uint32_t mw = is_act ? segw >> st::ACT_BITS : 0xFFFFu;
+        const uint32_t mw = is_act ? (uint32_t)S.nbw[ch][ct] : 0xFFFFu;
         const float w0 = pr.x * S.cohf[mw & 15u], w1 = pr.y * S.cohf[(mw >> 4) & 15u];
         const float w2 = pr.z * S.cohf[(mw >> 8) & 15u], w3 = pr.w * S.cohf[mw >> 12];
         float u = rfw * (w0 + w1 + w2 + w3);
@@ -771,18 +804,72 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
           else if (dd == 2u) py += 1.0f;
           else py -= 1.0f;
         }
-      } else if (rfz < mv0.w) {
+      } else if (z24 < th.w) {  // rfz < p_diff + p_settle
         py -= 1.0f;
       }
-      const int offx = rb_floor_i(px) - basex, offy = rb_floor_i(py) - basey;
+      const int2 bs = S.base[ct];
+      const int offx = rb_floor_i(px) - bs.x, offy = rb_floor_i(py) - bs.y;
       const uint32_t bi = (uint32_t)iclamp(offy, 0, 3) * 4u + (uint32_t)iclamp(offx, 0, 3);
       const uint16_t sl = S.slot[bi][ct];
       if (sl != st::FAR) {
         atomicAdd(&S.accum[ch][sl], unit);
       } else {
-        int tx = iclamp(cx + basex + (int)(bi & 3u), 0, (int)G - 1);
-        int ty = iclamp(cy + basey + (int)(bi >> 2), 0, (int)GH - 1);
+        const int tx = iclamp(X0 + (ct & 31) + bs.x + (int)(bi & 3u), 0, (int)G - 1);
+        const int ty = iclamp(cy + bs.y + (int)(bi >> 2), 0, (int)GH - 1);
         atomicAdd(d.chem_next + ((size_t)ty * G + tx) * 4 + ch, unit);
+      }
+    };
+
+    uint32_t cur = 0;  // the segment holding mover jb (warp-uniform)
+    uint32_t qn = 0;   // queued movers (warp-uniform)
+    for (uint32_t jb = 0; jb < total; jb += 32) {
+      const uint32_t j = jb + lane;
+      const bool valid = j < total;
+      // cur <= nseg - 1 <= NSEG - 1, so the entry read is below NSEG + 32 < SSTART
+      const uint32_t sc = sstart[cur + 1 + lane];
+      const uint32_t starts = __reduce_or_sync(0xffffffffu, sc < jb + 32u ? 1u << (sc - jb) : 0u);
+      const uint32_t s = cur + __popc(starts & le_mask);
+      cur += __popc(__ballot_sync(0xffffffffu, sc <= jb + 32u));
+      const uint2 r = rec[s];
+      const uint32_t k = j - (r.y & START_MASK);
+      const int ct = warp * 32 + (int)((r.y >> st::SEG_LANE_SHIFT) & 31u), ch = (int)((r.y >> st::SEG_CH_SHIFT) & 3u);
+      const float4 m0 = S.mv0[ct];
+      const uint4 th = S.thr[ct];
+      st::PcgHead ph = ph0;
+      ph.x1 = r.x;
+      const rb_u4 ru = st::pcg_draw(ph, st::pcg_z0(RB_S_MOVE + k));  // rb_pcg4d(slot, epoch, RB_S_MOVE + k, seed)
+      const uint32_t z24 = ru.z >> 8;
+      const bool gen = valid && z24 < th.y;  // hops (rfz < p_diff), or the cell takes the general path only
+      const uint32_t gm = __ballot_sync(0xffffffffu, gen);
+      if (gen) hq[qn + __popc(gm & lt_mask)] = (uint16_t)(s << 8 | k);
+      qn += __popc(gm);
+      if (valid && !gen) {
+        // no hop, no dispersion: bound or uniform start, displacement, settling
+        const bool is_act = k < (r.y >> st::SEG_ACT_SHIFT);
+        const uint32_t unit = is_act ? 1u : CHEM_SPENT_ONE;
+        const float p_bound = __uint_as_float(th.x);
+        const bool bound = is_act && p_bound > 0.0f &&
+                           rb_fract(rb_u2f(ru.z) * (float)7.31 + rb_u2f(ru.w) * (float)3.17) < p_bound;
+        const float px = (bound ? m0.z : rb_u2f(ru.x)) + m0.x;
+        float py = (bound ? m0.w : rb_u2f(ru.y)) + m0.y;
+        if (z24 < th.w) py -= 1.0f;  // rfz < p_diff + p_settle (and not below p_diff)
+        const int2 bs = S.base[ct];
+        const uint32_t bi = (uint32_t)((rb_floor_i(py) - bs.y) * 4 + (rb_floor_i(px) - bs.x));  // in [1, 10]
+        const uint16_t sl = S.slot[bi][ct];
+        if (sl != st::FAR) {
+          atomicAdd(&S.accum[ch][sl], unit);
+        } else {
+          const int tx = iclamp(X0 + (ct & 31) + bs.x + (int)(bi & 3u), 0, (int)G - 1);
+          const int ty = iclamp(cy + bs.y + (int)(bi >> 2), 0, (int)GH - 1);
+          atomicAdd(d.chem_next + ((size_t)ty * G + tx) * 4 + ch, unit);
+        }
+      }
+      // the queue holds at most HQ - 32 movers before a step adds up to 32
+      if (qn > (uint32_t)(st::HQ - 32) || jb + 32u >= total) {
+        __syncwarp();
+        for (uint32_t q = lane; q < qn; q += 32) general(hq[q]);
+        __syncwarp();
+        qn = 0;
       }
     }
   }
