@@ -118,6 +118,7 @@ std::string class_key(const World& w, uint32_t sched) {
   put(w.cfg.mg_pre);
   put(w.cfg.mg_post);
   put(w.cfg.mg_coarse);
+  put(w.cfg.precision_mode);
   return k;
 }
 
@@ -335,7 +336,9 @@ void Batch::plan_mg(Group* g) {
   if (g->mg_built) return;
   g->mg_built = true;
   const World& w0 = *worlds[g->members[0]];
-  if (!w0.st.multigrid || w0.st.mg_unfused) return;
+  // mixed-precision members solve one by one (their solver loops on its own
+  // convergence test per world)
+  if (w0.mixed || !w0.st.multigrid || w0.st.mg_unfused) return;
   const MgConfig c{(int)w0.cfg.mg_pre, (int)w0.cfg.mg_post, (int)w0.cfg.mg_coarse,
                    (int)(w0.st.mg_cycles < 1 ? 1 : w0.st.mg_cycles)};
   std::vector<MgWorld> mw;
@@ -586,6 +589,13 @@ ribo_status Batch::step(const ribo_sim_params* per_step, uint32_t n, const uint3
   }
   if (table_error) return set_error(RIBO_OOM, "batch tables: out of device memory");
   last_steps = n;
+  for (World* w : worlds) {  // a mixed-precision solve that failed to record
+    if (w->solve_error != RIBO_OK) {
+      const ribo_status s = w->solve_error;
+      for (World* v : worlds) v->solve_error = RIBO_OK;
+      return s;
+    }
+  }
   RB_TRY(cudaGetLastError(), "batch step launch");
   RB_TRY(cudaEventRecord(t1, stream), "event");
   return RIBO_OK;
@@ -611,7 +621,7 @@ ribo_status Batch::autotune(uint32_t* modes_out) {
   const MgConfig c{(int)w0.cfg.mg_pre, (int)w0.cfg.mg_post, (int)w0.cfg.mg_coarse, 1};
   std::vector<MgWorld> mw;
   for (World* w : worlds) {
-    if (w->cfg.mg_pre != w0.cfg.mg_pre || w->cfg.mg_post != w0.cfg.mg_post) continue;
+    if (w->mixed || w->cfg.mg_pre != w0.cfg.mg_pre || w->cfg.mg_post != w0.cfg.mg_post) continue;
     if (!multigrid_fused_ok(w->levels.data(), (int)w->levels.size(), c)) continue;
     mw.push_back(MgWorld{w->dev(), w->levels.data(), (int)w->levels.size(), w->mg});
   }
@@ -705,7 +715,6 @@ ribo_status ribo_batch_add(ribo_batch* b, ribo_world* w) {
   ribo::World& wd = w->w;
   if (wd.batch) return set_error(RIBO_INVALID_ARG, "world already belongs to a batch");
   if ((int)wd.cfg.device != b->b.device) return set_error(RIBO_INVALID_ARG, "world lives on another device");
-  if (wd.cfg.precision_mode != RIBO_PRECISION_F32) return set_error(RIBO_INVALID_ARG, "batches take f32-mode worlds");
   ribo_status st = ribo::cuda_status(b->b.bind(), "device");
   if (st != RIBO_OK) return st;
   st = ribo::cuda_status(cudaStreamSynchronize(wd.stream), "sync");

@@ -109,7 +109,6 @@ ribo_status Server::submit(const ribo_job& jd, uint64_t* id) {
   if (jd.steps == 0) return set_error(RIBO_INVALID_ARG, "job with 0 steps");
   if (jd.world.device != cfg.device) return set_error(RIBO_INVALID_ARG, "job world on device %u, server on %u",
                                                       jd.world.device, cfg.device);
-  if (jd.world.precision_mode != RIBO_PRECISION_F32) return set_error(RIBO_INVALID_ARG, "served jobs run in f32 mode");
   uint64_t fp = 0;
   ribo_status st = ribo_world_footprint(&jd.world, &fp);
   if (st != RIBO_OK) return st;

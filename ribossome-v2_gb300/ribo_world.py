@@ -142,6 +142,8 @@ def load_library(path: str = LIB_PATH):
         "ribo_derive_step_params": ([P(SimParams), P(WorldSettings), ctypes.c_uint32, P(SimParams)], ctypes.c_int),
         "ribo_world_ledger": ([vp, P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_world_sync": ([vp], ctypes.c_int),
+        "ribo_world_raise_status": ([vp, ctypes.c_uint32], ctypes.c_int),
+        "ribo_selftest_bounded_wait": ([ctypes.c_uint32, ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
         "ribo_world_last_step_ms": ([vp, P(ctypes.c_float)], ctypes.c_int),
         "ribo_world_enable_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "ribo_world_read_kernel_timing": ([vp, P(KernelTiming), ctypes.c_uint32, P(ctypes.c_uint32)], ctypes.c_int),
@@ -619,12 +621,14 @@ class Server:
 
     def submit(self, grid, fluid=None, *, steps: int, params: SimParams, settings: WorldSettings = None,
                inputs: dict = None, outputs=(), mg_min_size: int = 8, mg_pre: int = 2, mg_post: int = 2,
-               mg_coarse: int = 30, user_tag: int = 0) -> int:
-        """Queues a job; `outputs` lists the fields returned with its result."""
+               mg_coarse: int = 30, user_tag: int = 0, precision_mode: int = 0) -> int:
+        """Queues a job; `outputs` lists the fields returned with its result.
+        precision_mode 1 solves every step's pressure to the mixed-precision
+        tolerance."""
         gw, gh = (grid, grid) if isinstance(grid, int) else grid
         fw, fh = (gw, gh) if fluid is None else ((fluid, fluid) if isinstance(fluid, int) else fluid)
         j = Job()
-        j.world = WorldCfg(gw, gh, fw, fh, 30, mg_min_size, mg_pre, mg_post, mg_coarse, 0, self.device, 0)
+        j.world = WorldCfg(gw, gh, fw, fh, 30, mg_min_size, mg_pre, mg_post, mg_coarse, precision_mode, self.device, 0)
         j.settings = settings if settings is not None else default_settings()
         j.params = params
         j.steps = steps

@@ -72,6 +72,31 @@ def test_mixed_batch_equals_alone(rw):
     b.close()
 
 
+def test_mixed_precision_members_equal_alone(rw):
+    # Members that solve every step's pressure to the mixed-precision
+    # tolerance share the batch's launches with f32 members (their solves run
+    # one world at a time) and get the bits they get alone: pressure pair,
+    # velocity, transport.
+    specs = [(128, None, BASE, FULL, dict(MG33, precision_mode=1), {}),
+             ((256, 128), None, BASE, FULL, dict(MG33, precision_mode=1), dict(rock_frac=0.2)),
+             MIXED[0], MIXED[2]]
+    members, alone = twins(rw, specs)
+    b = rw.Batch(members)
+    for n in (1, 2, 2, 2):
+        b.encode_steps(n)
+        for w in alone:
+            w.encode_steps(n)
+        b.sync()
+        for k, (a, w) in enumerate(zip(members, alone)):
+            fields = STATE_FIELDS + ([(rw.PRESSURE_LO, "pressure_lo")] if k < 2 else [])
+            for f, name in fields:
+                assert_same(a.read(f), w.read(f), f"after a {n}-step call: member {k}: {name}")
+    for k in (0, 1):
+        outer, inner, rho = members[k].solve_info()
+        assert rho <= 1e-5, (k, outer, inner, rho)
+    b.close()
+
+
 def test_batch_members_match_oracle(rw, ro):
     specs = [MIXED[3], MIXED[4], MIXED[6]]
     members = [make_world(rw, s, 77 + i) for i, s in enumerate(specs)]

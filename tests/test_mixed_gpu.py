@@ -93,8 +93,6 @@ def test_mixed_mode_rejections(rw):
     with pytest.raises(rw.RiboError):
         rw.World((2048, 256), mg_min_size=16, precision_mode=MIXED)  # coarsest level 128x16, above 1024 cells
     w = mixed_world(rw, 256)
-    with pytest.raises(rw.RiboError):
-        rw.Batch([w])  # batches take f32-mode worlds
     f = rw.World(128)
     with pytest.raises(rw.RiboError):
         f.solve_info()

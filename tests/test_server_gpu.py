@@ -89,6 +89,40 @@ def test_served_jobs_equal_alone(rw):
     srv.close()
 
 
+def test_served_mixed_precision_jobs_equal_alone(rw):
+    # jobs that solve each pressure to the mixed-precision tolerance, served
+    # side by side with an f32 job, finish with the bits they get alone
+    base = (rw.CHEM, rw.VELOCITY, rw.PRESSURE, rw.DIVERGENCE)
+    specs = [((128, 128), 9, 1), ((192, 96), 6, 1), ((128, 128), 7, 0)]
+    srv = rw.Server(1 << 34, max_chunk_steps=4)
+    jobs = {}
+    for i, (grid, steps, mode) in enumerate(specs):
+        inputs = synth.make_world_inputs(grid, seed=4000 + i)
+        params = synth.bench_params(4000 + i)
+        st = rw.default_settings()
+        st.fluid_substep = 1
+        st.mg_cycles = 2
+        fields = base + ((rw.PRESSURE_LO,) if mode else ())
+        jid = srv.submit(grid, steps=steps, params=params, settings=st, inputs=inputs, outputs=fields,
+                         mg_min_size=16, mg_pre=3, mg_post=3, user_tag=i, precision_mode=mode)
+        jobs[i] = (grid, steps, mode, inputs, params, st, fields)
+    srv.drain()
+    results = srv.results()
+    assert len(results) == len(specs)
+    for r, outs in results:
+        assert r.status == 0
+        grid, steps, mode, inputs, params, st, fields = jobs[r.user_tag]
+        w = rw.World(grid, seed=1, mg_min_size=16, mg_pre=3, mg_post=3, precision_mode=mode)
+        w.seed_inputs(inputs)
+        w.params = params.copy()
+        w.settings = st
+        w.run(steps)
+        for f in fields:
+            assert_same(outs[f], w.read(f), f"job {r.user_tag} field {f}")
+        w.close()
+    srv.close()
+
+
 def test_over_budget_job_is_refused(rw):
     srv = rw.Server(10 * 1024 * 1024, max_chunk_steps=4)
     with pytest.raises(rw.RiboError) as e:
