@@ -321,7 +321,22 @@ ribo_status ribo_world_mark(ribo_world* w, uint32_t slot);
 ribo_status ribo_world_elapsed_ms(ribo_world* w, uint32_t slot_a, uint32_t slot_b, float* ms);
 
 // Waits until all work recorded on the world's stream has finished.
+// Kernels do not trap: a wait that gave up (a TMA that never completed)
+// sets a bit in the world's status word, which this call reads and clears,
+// returning RIBO_TIMEOUT (the last steps' results are then invalid).
 ribo_status ribo_world_sync(ribo_world* w);
+
+// Diagnostics (no counterpart in the reference).  ribo_world_raise_status
+// ORs `bits` into the world's status word on its stream, as a kernel whose
+// wait gave up would: the next ribo_world_sync reports RIBO_TIMEOUT (host
+// side of the error path, testable without a GPU fault).
+// ribo_selftest_bounded_wait runs one CTA on `device` that waits, at most
+// `polls` polls, on an mbarrier phase that nothing completes, the form every
+// TMA wait of the library takes; it stores the status bits the kernel
+// recorded (RIBO_ERR_TIMEOUT = 1 expected) in *status_bits and returns
+// RIBO_OK when the context is still usable afterwards.
+ribo_status ribo_world_raise_status(ribo_world* w, uint32_t bits);
+ribo_status ribo_selftest_bounded_wait(uint32_t device, uint32_t polls, uint32_t* status_bits);
 
 // Device time of the last ribo_world_step / encode_steps call, in ms (CUDA
 // events on the world's stream; waits for it).

@@ -3,6 +3,8 @@
 // one thread per fluid cell, with the same float operation order.
 #include "ribo_dev.cuh"
 #include "ribo_launch.h"
+#include "ribo_tma.cuh"
+#include "ribo_world_impl.h"
 
 namespace ribo {
 
@@ -564,7 +566,38 @@ __global__ void k_smooth(const __grid_constant__ S s, int dir) {
   }
 }
 
+// One CTA that waits on an mbarrier phase nothing completes (one arrival
+// expected, with 16 bytes of transactions that no copy delivers): the wait
+// gives up after `polls` polls and records a timeout, as a kernel's bounded
+// wait on a bulk copy would.
+__global__ void k_selftest_bounded_wait(uint32_t polls, uint32_t* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_arrive_expect(&bar, 16u);
+  }
+  __syncthreads();
+  const bool late = !mbar_wait(&bar, 0u, polls);
+  if (__syncthreads_or(late) && threadIdx.x == 0) atomicOr(status, ERR_TIMEOUT);
+}
+
 }  // namespace
+
+ribo_status selftest_bounded_wait(int device, uint32_t polls, uint32_t* bits) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_status(e, "device");
+  uint32_t* d_status = nullptr;
+  e = cudaMalloc((void**)&d_status, 4);
+  if (e != cudaSuccess) return cuda_status(e, "selftest");
+  e = cudaMemset(d_status, 0, 4);
+  if (e == cudaSuccess) {
+    k_selftest_bounded_wait<<<1, 32>>>(polls, d_status);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(bits, d_status, 4, cudaMemcpyDeviceToHost);
+  cudaFree(d_status);
+  return cuda_status(e, "selftest");
+}
 
 void launch_solid_mask(const Target& t, cudaStream_t s) {
   const dim3 blk(BX, BY);

@@ -150,6 +150,8 @@ void launch_subtract_gradient(const Target& t, int dir, cudaStream_t s);
 void launch_net_flux(const Target& t, int dir, cudaStream_t s);
 void launch_boundaries(const Target& t, int dir, cudaStream_t s);
 void launch_smooth(const Target& t, int dir, cudaStream_t s);
+// A bounded mbarrier wait that runs out, on `device` (ribo_selftest_bounded_wait).
+ribo_status selftest_bounded_wait(int device, uint32_t polls, uint32_t* bits);
 
 // multigrid.cu
 struct MgLevel {

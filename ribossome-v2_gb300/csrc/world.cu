@@ -693,7 +693,9 @@ ribo_status World::check_status() {
   RB_TRY(cudaStreamSynchronize(stream), "status");
   if (h) {
     RB_TRY(cudaMemsetAsync(status, 0, 4, stream), "status");
-    return set_error(RIBO_TIMEOUT, "a kernel wait timed out (status 0x%x); results of the last steps are invalid", h);
+    if (h & ERR_TIMEOUT)
+      return set_error(RIBO_TIMEOUT, "a kernel wait timed out (status 0x%x); results of the last steps are invalid", h);
+    return set_error(RIBO_CUDA_ERROR, "a kernel index check failed (status 0x%x); results of the last steps are invalid", h);
   }
   return RIBO_OK;
 }
@@ -1013,6 +1015,28 @@ ribo_status ribo_world_sync(ribo_world* w) {
   ribo_status st = ribo::cuda_status(cudaStreamSynchronize(w->w.stream), "sync");
   if (st != RIBO_OK) return st;
   return w->w.check_status();
+}
+
+ribo_status ribo_world_raise_status(ribo_world* w, uint32_t bits) {
+  if (!w) return set_error(RIBO_INVALID_ARG, "null world");
+  using ribo::cuda_status;
+  RB_TRY(w->w.bind(), "device");
+  uint32_t cur = 0;
+  RB_TRY(cudaMemcpyAsync(&cur, w->w.status, 4, cudaMemcpyDeviceToHost, w->w.stream), "status");
+  RB_TRY(cudaStreamSynchronize(w->w.stream), "status");
+  cur |= bits;
+  RB_TRY(cudaMemcpyAsync(w->w.status, &cur, 4, cudaMemcpyHostToDevice, w->w.stream), "status");
+  RB_TRY(cudaStreamSynchronize(w->w.stream), "status");
+  return RIBO_OK;
+}
+
+ribo_status ribo_selftest_bounded_wait(uint32_t device, uint32_t polls, uint32_t* status_bits) {
+  if (!status_bits) return set_error(RIBO_INVALID_ARG, "null argument");
+  *status_bits = 0;
+  ribo_status st = ribo::selftest_bounded_wait((int)device, polls, status_bits);
+  if (st != RIBO_OK) return st;
+  // the context still answers: a trivial synchronous call after the kernel
+  return ribo::cuda_status(cudaDeviceSynchronize(), "selftest");
 }
 
 ribo_status ribo_world_enable_kernel_timing(ribo_world* w, int enable) {
