@@ -48,32 +48,49 @@ def headers():
     return hs
 
 
-def _compile(src: str, extra) -> str:
-    obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
+# The bounds-checked variant: kernels test their riskiest indices and record
+# RIBO_ERR_BOUNDS in the world's status word instead of accessing out of
+# range (ribo_world_sync then fails); a separate library for test runs.
+CHECKED_DIR = os.path.join(OUT_DIR, "checked")
+CHECKED_LIB = os.path.join(CHECKED_DIR, "libribo_world.so")
+CHECKED_FLAGS = ("-DRB_BOUNDS_CHECK",)
+
+
+def _compile(src: str, extra, out_dir: str, force: bool) -> str:
+    obj = os.path.join(out_dir, os.path.basename(src) + ".o")
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in headers()])
-    if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep and not extra:
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep and not force:
         return obj
     cmd = [nvcc()] + NVCC_FLAGS + list(extra) + ["-c", src, "-o", obj]
     subprocess.run(cmd, check=True)
     return obj
 
 
-def build(verbose: bool = False, extra=()) -> str:
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(verbose: bool = False, extra=(), checked: bool = False) -> str:
+    """Builds the library (or, with checked=True, the bounds-checked variant
+    in _build/checked/); extra flags force a rebuild of the default one."""
+    out_dir, lib = (CHECKED_DIR, CHECKED_LIB) if checked else (OUT_DIR, LIB)
+    flags = tuple(extra) + (CHECKED_FLAGS if checked else ())
+    force = bool(extra)
+    os.makedirs(out_dir, exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
-    if os.path.exists(LIB) and not extra:
-        t = os.path.getmtime(LIB)
+        objs = list(ex.map(lambda s: _compile(s, flags, out_dir, force), srcs))
+    if os.path.exists(lib) and not force:
+        t = os.path.getmtime(lib)
         if all(os.path.getmtime(o) <= t for o in objs):
-            return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs
+            return lib
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs
     subprocess.run(cmd, check=True)
-    os.replace(LIB + ".tmp", LIB)
+    os.replace(lib + ".tmp", lib)
     if verbose:
-        print(LIB)
-    return LIB
+        print(lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, extra=sys.argv[1:]))
+    args = sys.argv[1:]
+    if args[:1] == ["--checked"]:
+        print(build(verbose=True, extra=args[1:], checked=True))
+    else:
+        print(build(verbose=True, extra=args))

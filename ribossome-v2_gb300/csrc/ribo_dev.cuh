@@ -288,6 +288,21 @@ __device__ __forceinline__ float light_absorbed_at(const Dev& d, const ribo_sim_
 // Status words written by kernels instead of trapping.
 enum : uint32_t { ERR_NONE = 0, ERR_TIMEOUT = 1, ERR_BOUNDS = 2 };
 
+// Index checks of the bounds-checked build (-DRB_BOUNDS_CHECK): RB_IN(i, n)
+// is true when 0 <= i < n; otherwise it records ERR_BOUNDS in the world's
+// status word and is false, and the caller skips the access.  In the normal
+// build it is always true and costs nothing.
+#ifdef RB_BOUNDS_CHECK
+__device__ __forceinline__ bool rb_in_bounds(long long i, long long n, uint32_t* status) {
+  if (i >= 0 && i < n) return true;
+  if (status) atomicOr(status, ERR_BOUNDS);
+  return false;
+}
+#define RB_IN(i, n, status) ::ribo::rb_in_bounds((long long)(i), (long long)(n), (status))
+#else
+#define RB_IN(i, n, status) true
+#endif
+
 // ---- Where a CTA works ------------------------------------------------------
 // Block shapes of the passes, shared by the kernels and by the host code that
 // sizes batched launches.

@@ -812,11 +812,12 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       const uint32_t bi = (uint32_t)iclamp(offy, 0, 3) * 4u + (uint32_t)iclamp(offx, 0, 3);
       const uint16_t sl = S.slot[bi][ct];
       if (sl != st::FAR) {
-        atomicAdd(&S.accum[ch][sl], unit);
+        if (RB_IN(sl, st::AC, d.status)) atomicAdd(&S.accum[ch][sl], unit);
       } else {
         const int tx = iclamp(X0 + (ct & 31) + bs.x + (int)(bi & 3u), 0, (int)G - 1);
         const int ty = iclamp(cy + bs.y + (int)(bi >> 2), 0, (int)GH - 1);
-        atomicAdd(d.chem_next + ((size_t)ty * G + tx) * 4 + ch, unit);
+        const size_t t = ((size_t)ty * G + tx) * 4 + ch;
+        if (RB_IN(t, (size_t)G * GH * 4, d.status)) atomicAdd(d.chem_next + t, unit);
       }
     };
 
@@ -826,7 +827,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       const uint32_t j = jb + lane;
       const bool valid = j < total;
       // cur <= nseg - 1 <= NSEG - 1, so the entry read is below NSEG + 32 < SSTART
-      const uint32_t sc = sstart[cur + 1 + lane];
+      const uint32_t sc = RB_IN(cur + 1 + lane, st::SSTART, d.status) ? sstart[cur + 1 + lane] : st::NO_START;
       const uint32_t starts = __reduce_or_sync(0xffffffffu, sc < jb + 32u ? 1u << (sc - jb) : 0u);
       const uint32_t s = cur + __popc(starts & le_mask);
       cur += __popc(__ballot_sync(0xffffffffu, sc <= jb + 32u));
@@ -841,7 +842,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       const uint32_t z24 = ru.z >> 8;
       const bool gen = valid && z24 < th.y;  // hops (rfz < p_diff), or the cell takes the general path only
       const uint32_t gm = __ballot_sync(0xffffffffu, gen);
-      if (gen) hq[qn + __popc(gm & lt_mask)] = (uint16_t)(s << 8 | k);
+      if (gen && RB_IN(qn + __popc(gm & lt_mask), st::HQ, d.status)) hq[qn + __popc(gm & lt_mask)] = (uint16_t)(s << 8 | k);
       qn += __popc(gm);
       if (valid && !gen) {
         // no hop, no dispersion: bound or uniform start, displacement, settling
@@ -855,13 +856,16 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         if (z24 < th.w) py -= 1.0f;  // rfz < p_diff + p_settle (and not below p_diff)
         const int2 bs = S.base[ct];
         const uint32_t bi = (uint32_t)((rb_floor_i(py) - bs.y) * 4 + (rb_floor_i(px) - bs.x));  // in [1, 10]
-        const uint16_t sl = S.slot[bi][ct];
-        if (sl != st::FAR) {
-          atomicAdd(&S.accum[ch][sl], unit);
-        } else {
-          const int tx = iclamp(X0 + (ct & 31) + bs.x + (int)(bi & 3u), 0, (int)G - 1);
-          const int ty = iclamp(cy + bs.y + (int)(bi >> 2), 0, (int)GH - 1);
-          atomicAdd(d.chem_next + ((size_t)ty * G + tx) * 4 + ch, unit);
+        if (RB_IN(bi, 16, d.status)) {
+          const uint16_t sl = S.slot[bi][ct];
+          if (sl != st::FAR) {
+            if (RB_IN(sl, st::AC, d.status)) atomicAdd(&S.accum[ch][sl], unit);
+          } else {
+            const int tx = iclamp(X0 + (ct & 31) + bs.x + (int)(bi & 3u), 0, (int)G - 1);
+            const int ty = iclamp(cy + bs.y + (int)(bi >> 2), 0, (int)GH - 1);
+            const size_t t = ((size_t)ty * G + tx) * 4 + ch;
+            if (RB_IN(t, (size_t)G * GH * 4, d.status)) atomicAdd(d.chem_next + t, unit);
+          }
         }
       }
       // the queue holds at most HQ - 32 movers before a step adds up to 32
@@ -881,7 +885,8 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
     uint32_t v = S.accum[ch][cell];
     if (!v) continue;
     int gx = X0 - st::HALO + cell % st::AW, gy = Y0 - st::HALO + cell / st::AW;
-    atomicAdd(d.chem_next + ((size_t)gy * G + gx) * 4 + ch, v);
+    // only in-grid destinations receive monomers (the slots are clamped to the grid)
+    if (RB_IN(gx, G, d.status) && RB_IN(gy, GH, d.status)) atomicAdd(d.chem_next + ((size_t)gy * G + gx) * 4 + ch, v);
   }
 }
 
