@@ -22,6 +22,31 @@ def declared_functions():
     return sorted(set(names))
 
 
+def c_struct_fields(name):
+    text = open(os.path.join(ROOT, "include", "ribo_world.h")).read()
+    body = re.search(r"typedef struct " + name + r" \{(.*?)\} " + name + ";", text, re.S).group(1)
+    fields = []
+    for line in body.splitlines():
+        line = line.split("//")[0].strip()
+        if not line:
+            continue
+        decl = line.rstrip(";").split(None, 1)[1]
+        fields += [re.sub(r"\[.*\]", "", f).strip() for f in decl.split(",")]
+    return fields
+
+
+def test_rust_binding_matches_header():
+    """The Rust binding (rust/src/lib.rs) declares only functions the header
+    declares, and its mirrored structs have the header's fields in order."""
+    rs = open(os.path.join(ROOT, "rust", "src", "lib.rs")).read()
+    fns = re.findall(r"pub fn (ribo_\w+)\(", rs)
+    assert fns and not [f for f in fns if f not in declared_functions()]
+    for c_name, rs_name in (("ribo_world_cfg", "RiboWorldCfg"), ("ribo_world_settings", "RiboWorldSettings")):
+        body = re.search(r"pub struct " + rs_name + r" \{(.*?)\}", rs, re.S).group(1)
+        rs_fields = re.findall(r"pub (\w+):", body)
+        assert rs_fields == c_struct_fields(c_name), (c_name, rs_fields, c_struct_fields(c_name))
+
+
 def test_header_declares_entry_points():
     names = declared_functions()
     for n in ("ribo_world_create", "ribo_world_step", "ribo_world_encode_steps", "ribo_world_ledger",
