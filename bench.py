@@ -432,6 +432,8 @@ def run_ours(args):
     if ws == 1 and not args.no_batched:
         w.close()
         line["batched"] = run_batched(args, local)
+        if not args.no_mixed and args.batched_mixed_steps > 0:
+            line["batched"]["mixed"] = run_batched(args, local, precision_mode=1, steps=args.batched_mixed_steps)
     if ws == 1 and not args.no_serving:
         line["serving"] = run_serving(args, local, args.serve_rate, args.serve_seconds, args.serve_drain_seconds)
         if args.serve_sustainable_rate > 0:
@@ -492,7 +494,7 @@ def percentile(xs, q):
     return s[lo] + (s[hi] - s[lo]) * (k - lo)
 
 
-def run_batched(args, local):
+def run_batched(args, local, precision_mode=0, steps=None):
     """Batched worlds vs the plain per-world loop on the same GPU.
 
     64 worlds of uneven sizes (synth.batch_specs: squares 128..1024 and the
@@ -503,7 +505,10 @@ def run_batched(args, local):
     one launch over all of them, steps replayed from CUDA graphs.
     Throughput = world-steps / device time; latency = device time of one
     step as its caller sees it (one world's step alone, or one batched step
-    that advances every world).
+    that advances every world).  precision_mode 1: every world solves every
+    step's pressure to a relative residual of 1e-5 (mixed precision); the
+    batch runs those solves one world at a time inside its step, and every
+    world's last residual is checked against the tolerance.
     """
     import ribo_world as rw
     import synth
@@ -512,7 +517,10 @@ def run_batched(args, local):
     worlds = []
     total_cells = 0
     for (gw, gh), seed, rock, mean in specs:
-        w = rw.World((gw, gh), seed=seed, mg_min_size=16, mg_pre=3, mg_post=3, device=local)
+        # the FP64 dense coarsest solve takes at most 1024 cells: the mixed
+        # hierarchy goes down to 8 (2048x256 would stop at 128x16 with 16)
+        w = rw.World((gw, gh), seed=seed, mg_min_size=8 if precision_mode else 16, mg_pre=3, mg_post=3,
+                     device=local, precision_mode=precision_mode)
         w.settings.fluid_substep = 1
         w.settings.mg_cycles = 4
         w.seed_inputs(synth.make_world_inputs((gw, gh), seed=seed, rock_frac=rock, monomer_mean=mean))
@@ -520,7 +528,7 @@ def run_batched(args, local):
         worlds.append(w)
         total_cells += gw * gh
     seeded = [w.ledger_blocking().total() for w in worlds]
-    steps = args.batched_steps
+    steps = steps or args.batched_steps
     warm = max(args.warmup, 3)
 
     # ---- plain per-world loop ----
@@ -568,6 +576,11 @@ def run_batched(args, local):
     for w, s0 in zip(worlds, seeded):
         if w.ledger_blocking().total() != s0:
             raise RuntimeError("matter not conserved (batched)")
+    worst = None
+    if precision_mode:
+        worst = max(w.solve_info()[2] for w in worlds)
+        if not worst <= 1e-5:
+            raise RuntimeError(f"batched mixed-precision solve above tolerance: {worst}")
     n = len(worlds)
     plain = {"world_steps_per_s": n * steps / (plain_ms / 1000.0), "wall_world_steps_per_s": n * steps / plain_wall,
              "step_latency_ms_p50": percentile(plain_lat, 50), "step_latency_ms_p99": percentile(plain_lat, 99)}
@@ -576,14 +589,19 @@ def run_batched(args, local):
                "gpu_launches": launches, "tile_modes": modes}
     for w in worlds:
         w.close()
-    return {
+    solver = ("every pressure solved to relative residual 1e-5 (mixed precision, 3+3 V-cycles to 8x8 as "
+              "the preconditioner)" if precision_mode else "4 V-cycles 3+3 to 16x16")
+    out = {
         "workload": f"{n} worlds of uneven sizes (seeded draw from squares 128..1024 and 512x2048, 2048x256; "
-                    f"{total_cells / 1e6:.1f} M cells), 4 V-cycles 3+3 to 16x16, transport every step, "
+                    f"{total_cells / 1e6:.1f} M cells), {solver}, transport every step, "
                     f"{steps} steps each",
         "worlds": n, "steps": steps, "cells": total_cells, "plain": plain, "batched": batched,
         "speedup": batched["world_steps_per_s"] / plain["world_steps_per_s"],
         "latency_note": "plain: one world's step alone; batched: one batched step (advances every world)",
     }
+    if precision_mode:
+        out["worst_rel_residual_device"] = worst
+    return out
 
 
 def run_extras(args, w):
@@ -958,6 +976,7 @@ def main():
     ap.add_argument("--reference-seconds", type=float, default=60.0)
     ap.add_argument("--batched-worlds", type=int, default=64)
     ap.add_argument("--batched-steps", type=int, default=200)
+    ap.add_argument("--batched-mixed-steps", type=int, default=24)
     ap.add_argument("--latency-samples", type=int, default=5)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
