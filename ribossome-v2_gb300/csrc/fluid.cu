@@ -1,6 +1,8 @@
 // Fluid passes of the world step (stable fluids at fluid resolution).
 // Each kernel restates one WGSL entry point of shaders/world/fluid.wgsl,
 // one thread per fluid cell, with the same float operation order.
+#include <mutex>
+
 #include "ribo_dev.cuh"
 #include "ribo_launch.h"
 #include "ribo_tma.cuh"
@@ -189,12 +191,23 @@ __device__ __forceinline__ float2 slope_steer(const Dev& d, const ribo_sim_param
 
 // fluid.wgsl:410-432 (add_forces; clear_forces is dropped: gather
 // overwrites every fluid_forces entry before the next read)
+// The gathered forces of the tile and its ring are staged in shared memory
+// (a TMA box), so the 3 x 3 average reads them there.
 template <class S>
 __global__ void k_add_forces(const __grid_constant__ S s, int dir) {
   RB_WORLD(s);
+  __shared__ __align__(128) uint2 FB[ST_BOX];
+  __shared__ uint64_t bar;
+  const int x0 = (int)(cta.bx * BX), y0 = (int)(cta.by * BY);
+  {
+    const int map[1] = {SM_FORCES};
+    const uint2* const src[1] = {reinterpret_cast<const uint2*>(d.forces)};
+    uint2* const box[1] = {FB};
+    if (!stage_stencil<1>(d.tmap, map, src, box, x0, y0, d.fw, d.fh, &bar, d.status)) return;
+  }
   const float2* __restrict__ vin = dir ? d.vb : d.va;
   float2* __restrict__ vout = dir ? d.va : d.vb;
-  uint32_t x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
+  uint32_t x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   if (x >= (uint32_t)d.fw || y >= (uint32_t)d.fh) return;
   const int fw = d.fw;
   size_t idx = (size_t)y * fw + x;
@@ -204,7 +217,8 @@ __global__ void k_add_forces(const __grid_constant__ S s, int dir) {
   const float dt = fluid_dt(P);
   uint32_t xm = x > 0u ? x - 1u : x, xp = x + 1u < (uint32_t)fw ? x + 1u : x;
   uint32_t ym = y > 0u ? y - 1u : y, yp = y + 1u < (uint32_t)d.fh ? y + 1u : y;
-  auto F = [&](uint32_t a, uint32_t b) { return sanitize(__ldg(d.forces + (size_t)b * fw + a)); };
+  const float2* Ff = reinterpret_cast<const float2*>(FB);
+  auto F = [&](uint32_t a, uint32_t b) { return sanitize(Ff[st_at(x0, y0, (int)a, (int)b)]); };
   float2 f_c = F(x, y);
   float2 axis = add2(add2(add2(F(xm, y), F(xp, y)), F(x, ym)), F(x, yp));
   float2 diag = add2(add2(add2(F(xm, ym), F(xp, ym)), F(xm, yp)), F(xp, yp));
@@ -597,6 +611,48 @@ ribo_status selftest_bounded_wait(int device, uint32_t polls, uint32_t* bits) {
   if (e == cudaSuccess) e = cudaMemcpy(bits, d_status, 4, cudaMemcpyDeviceToHost);
   cudaFree(d_status);
   return cuda_status(e, "selftest");
+}
+
+// One descriptor per staged 8-byte field: dimensions (fw, fh), row pitch
+// fw * 8 bytes, the ST_BW x ST_BH box, zero fill outside the field.  The pitch
+// must be a multiple of 16 bytes (fw even), the fields 16-byte aligned and the
+// descriptors' home 64-byte aligned; otherwise the passes use plain loads.
+bool stencil_tensor_maps(void* dst, const StencilFields& f, cudaStream_t s) {
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                              const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<Encode>(fn);
+    cudaGetLastError();
+  });
+  if (!encode || f.fw % 2 != 0 || f.fw < 1 || f.fh < 1 || (reinterpret_cast<uintptr_t>(dst) & 63u)) return false;
+  const void* fields[SM_COUNT] = {f.forces};
+  static_assert(STENCIL_TMAP_BYTES == SM_COUNT * sizeof(CUtensorMap) && STENCIL_TMAP_BYTES == STENCIL_TMAP_BYTES_HOST,
+                "one descriptor per field");
+  CUtensorMap maps[SM_COUNT];
+  const cuuint64_t dims[2] = {(cuuint64_t)f.fw, (cuuint64_t)f.fh};
+  const cuuint64_t pitch[1] = {(cuuint64_t)f.fw * 8u};
+  const cuuint32_t box[2] = {(cuuint32_t)ST_BW, (cuuint32_t)ST_BH};
+  const cuuint32_t unit[2] = {1u, 1u};
+  for (int k = 0; k < SM_COUNT; k++) {
+    if (reinterpret_cast<uintptr_t>(fields[k]) & 15u) return false;
+    if (encode(&maps[k], CU_TENSOR_MAP_DATA_TYPE_INT64, 2, const_cast<void*>(fields[k]), dims, pitch, box, unit,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  // pageable source: the call returns once the descriptors are staged
+  if (cudaMemcpyAsync(dst, maps, sizeof maps, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
 }
 
 void launch_solid_mask(const Target& t, cudaStream_t s) {

@@ -109,8 +109,9 @@ struct Dev {
   uint32_t* ledger;   // 12 words
   uint8_t* fluid0;    // level-0 water flags of the multigrid (1 = water), rebuilt with the mask
   uint32_t* status;   // error bits written by kernels instead of trapping (RIBO_ERR_*)
+  const void* tmap;   // TMA descriptors of the stencil passes' tiles (csrc/ribo_tma.cuh), or null
 };
-static_assert(sizeof(Dev) == 16 * 4 + 30 * sizeof(void*), "Dev has no padding bytes: every byte is a member");
+static_assert(sizeof(Dev) == 16 * 4 + 31 * sizeof(void*), "Dev has no padding bytes: every byte is a member");
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }

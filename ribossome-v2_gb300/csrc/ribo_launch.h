@@ -150,6 +150,16 @@ void launch_subtract_gradient(const Target& t, int dir, cudaStream_t s);
 void launch_net_flux(const Target& t, int dir, cudaStream_t s);
 void launch_boundaries(const Target& t, int dir, cudaStream_t s);
 void launch_smooth(const Target& t, int dir, cudaStream_t s);
+// TMA descriptors of a world's stencil-pass tiles (the gathered forces),
+// written to `dst` (device, STENCIL_TMAP_BYTES, 64-byte aligned) on stream
+// s; false where the field cannot be described (the pass then stages its
+// tile with plain loads).
+struct StencilFields {
+  const void* forces;
+  int fw, fh;
+};
+constexpr size_t STENCIL_TMAP_BYTES_HOST = 128;
+bool stencil_tensor_maps(void* dst, const StencilFields& f, cudaStream_t s);
 // A bounded mbarrier wait that runs out, on `device` (ribo_selftest_bounded_wait).
 ribo_status selftest_bounded_wait(int device, uint32_t polls, uint32_t* bits);
 

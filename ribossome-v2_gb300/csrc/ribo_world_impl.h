@@ -91,6 +91,7 @@ struct World {
   uint8_t* mask = nullptr;
   float2* normal = nullptr;
   float* curl = nullptr;
+  void* tmaps = nullptr;  // TMA descriptors of the stencil passes' tiles (null: plain loads)
   uint32_t* mask32 = nullptr;
   float2 *va = nullptr, *vb = nullptr, *vsmooth = nullptr;
   float *pa = nullptr, *pb = nullptr, *div = nullptr;

@@ -191,6 +191,7 @@ Dev World::dev() const {
   d.ledger = ledger;
   d.fluid0 = (mg.fluid && !levels.empty()) ? mg.fluid + levels[0].off : nullptr;
   d.status = status;
+  d.tmap = tmaps;
   return d;
 }
 
@@ -253,6 +254,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 * 2 + MAX_STEPS * 12 * 4 + 16;
   b += M * (4 + 4 + 1 + 4);                                       // mg p, rhs, fluid, p2
   b += 2 * MAX_STEPS * sizeof(ribo_sim_params);
+  b += STENCIL_TMAP_BYTES_HOST;                                   // TMA descriptor of the stencil passes
   if (c.precision_mode == RIBO_PRECISION_MIXED) b += mixed_footprint(c, lv);
   return b;
 }
@@ -326,6 +328,12 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(mg.p_tmp, F * 4);
   RB_ALLOC(mg.p2, mg_total * 4);
   RB_ALLOC(status, 16);
+  {
+    void* maps = nullptr;
+    RB_ALLOC(maps, STENCIL_TMAP_BYTES_HOST);
+    const StencilFields f{forces, fw, fh};
+    if (stencil_tensor_maps(maps, f, own_stream)) tmaps = maps;
+  }
   RB_ALLOC(d_params, 2 * MAX_STEPS * sizeof(ribo_sim_params));
 #undef RB_ALLOC
   RB_TRY(cudaMallocHost((void**)&h_params, 2 * MAX_STEPS * sizeof(ribo_sim_params) + 12 * 4), "pinned params");

@@ -30,6 +30,9 @@ CASES = [
                                               aggregation=0.02), dict(fluid_substep=1), 10, {}),
     ("jacobi-96", 96, None, BASE, dict(fluid_substep=1, multigrid=0, jacobi_iters=17), 4, {}),
     ("rect-128x64", (128, 64), None, BASE, dict(fluid_substep=1), 6, {}),
+    # an odd fluid width: a row pitch that no tensor map can describe, so the
+    # stencil tiles are staged with plain loads (one multigrid level)
+    ("odd-width-75x48", (150, 96), (75, 48), BASE, dict(fluid_substep=1), 5, {}),
     ("rect-64x128-half-fluid", (64, 128), (32, 64), dict(BASE, monomer_pressure=2.0), dict(fluid_substep=1), 6, {}),
     ("sparse-transport", 64, None, dict(dt=1.0, transport_every=3, aggregation=0.0), dict(fluid_substep=2), 9, {}),
     ("sun-and-vents", 64, None, dict(dt=0.05, sun_heat=1.0, day_period=400.0, activation_decay=0.01,
