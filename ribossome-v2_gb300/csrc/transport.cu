@@ -85,13 +85,16 @@ __global__ void k_agg_count(const __grid_constant__ S s) {
                      (c[r].w & CHEM_STATE_MASK);
   }
 }
-// transport.wgsl:71-87
+// transport.wgsl:71-87.  The scatter reads the neighbour count plus the
+// cell's own activated count (transport.wgsl:196-201); integer adds
+// commute, so agg_nb holds that sum directly: the 3 x 3 box of activated
+// counts.
 template <class S>
 __global__ void k_agg_neighbours(const __grid_constant__ S s) {
   RB_WORLD(s);
   int x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
   if (x >= d.gw || y >= d.gh) return;
-  uint32_t sum = 0;
+  uint32_t sum = d.agg_act[(size_t)y * d.gw + x];
   for (int dy = -1; dy <= 1; dy++)
     for (int dx = -1; dx <= 1; dx++) {
       if (dx == 0 && dy == 0) continue;
@@ -203,11 +206,11 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ S s) {
   float accept_spent[4] = {1.0f, 1.0f, 1.0f, 1.0f};
   if (P->aggregation > 0.0f && src_total <= cap_self) {
     float e[5];
-    e[0] = (float)(d.agg_nb[idx] + d.agg_act[idx]);
-    e[1] = x + 1u < G ? (float)(d.agg_nb[idx + 1] + d.agg_act[idx + 1]) : 0.0f;
-    e[2] = x > 0u ? (float)(d.agg_nb[idx - 1] + d.agg_act[idx - 1]) : 0.0f;
-    e[3] = y + 1u < GH ? (float)(d.agg_nb[idx + G] + d.agg_act[idx + G]) : 0.0f;
-    e[4] = y > 0u ? (float)(d.agg_nb[idx - G] + d.agg_act[idx - G]) : 0.0f;
+    e[0] = (float)d.agg_nb[idx];  // neighbours + own activated counts
+    e[1] = x + 1u < G ? (float)d.agg_nb[idx + 1] : 0.0f;
+    e[2] = x > 0u ? (float)d.agg_nb[idx - 1] : 0.0f;
+    e[3] = y + 1u < GH ? (float)d.agg_nb[idx + G] : 0.0f;
+    e[4] = y > 0u ? (float)d.agg_nb[idx - G] : 0.0f;
     uint32_t fx = umin((x * (uint32_t)d.fw) / G, (uint32_t)d.fw - 1u);
     uint32_t fy = umin((y * (uint32_t)d.fh) / GH, (uint32_t)d.fh - 1u);
     float t_rel = 1.0f + rb_max(d.temp_in[(size_t)fy * d.fw + fx], 0.0f) / TEMP_ACT_THRESHOLD;
@@ -532,7 +535,16 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       float2 v = f2(0.0f, 0.0f);
       if (P->fluid_enabled != 0u && g_src < GAMMA_SOLID) {
         float2 c = mul2(f2((float)x + 0.5f, (float)y + 0.5f), d.cell_w);
-        float2 v0 = fluid_velocity_at_world(d, c);
+        // On a world whose fluid grid is its environment grid, with power-of-
+        // two sides and sim sizes below 2^23, the first sample point lands
+        // exactly on the cell's own centre: ((x + 0.5) w) / (G w) is the exact
+        // (x + 0.5) / G, times G is x + 0.5, so the bilinear weights are 0 and
+        // the sample is the cell's own (sanitised) velocity, up to the sign of
+        // a zero component -- which cannot change c + v0 * wpf * h / 2 below
+        // (c > 0).  One load instead of the four-point sample.
+        const bool centred = d.gw == d.fw && d.gh == d.fh && (d.gw & (d.gw - 1)) == 0 && (d.gh & (d.gh - 1)) == 0 &&
+                             d.sim_w < 8388608.0f && d.sim_h < 8388608.0f;
+        float2 v0 = centred ? sanitize(d.va[idx]) : fluid_velocity_at_world(d, c);
         float h = rb_max(P->dt, 0.0f);
         float2 c2 = f2(c.x + v0.x * d.wpf_x * h * 0.5f, c.y + v0.y * d.wpf_y * h * 0.5f);
         v = fluid_velocity_at_world(d, c2);
@@ -599,11 +611,11 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       float acc[4] = {1.0f, 1.0f, 1.0f, 1.0f}, accs[4] = {1.0f, 1.0f, 1.0f, 1.0f};
       if (P->aggregation > 0.0f && src_total <= cap_self) {
         float e[5];
-        e[0] = (float)(d.agg_nb[idx] + d.agg_act[idx]);
-        e[1] = x + 1u < G ? (float)(d.agg_nb[idx + 1] + d.agg_act[idx + 1]) : 0.0f;
-        e[2] = x > 0u ? (float)(d.agg_nb[idx - 1] + d.agg_act[idx - 1]) : 0.0f;
-        e[3] = y + 1u < GH ? (float)(d.agg_nb[idx + G] + d.agg_act[idx + G]) : 0.0f;
-        e[4] = y > 0u ? (float)(d.agg_nb[idx - G] + d.agg_act[idx - G]) : 0.0f;
+        e[0] = (float)d.agg_nb[idx];  // neighbours + own activated counts
+        e[1] = x + 1u < G ? (float)d.agg_nb[idx + 1] : 0.0f;
+        e[2] = x > 0u ? (float)d.agg_nb[idx - 1] : 0.0f;
+        e[3] = y + 1u < GH ? (float)d.agg_nb[idx + G] : 0.0f;
+        e[4] = y > 0u ? (float)d.agg_nb[idx - G] : 0.0f;
         uint32_t fx = umin((x * (uint32_t)d.fw) / G, (uint32_t)d.fw - 1u);
         uint32_t fy = umin((y * (uint32_t)d.fh) / GH, (uint32_t)d.fh - 1u);
         float t_rel = 1.0f + rb_max(d.temp_in[(size_t)fy * d.fw + fx], 0.0f) / TEMP_ACT_THRESHOLD;
