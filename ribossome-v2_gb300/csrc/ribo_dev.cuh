@@ -4,6 +4,7 @@
 // pinned semantics of ribo_fmath.h (the library is compiled with
 // -fmad=false, IEEE division and square root).
 #pragma once
+#include <cstdio>  // device printf of the bounds-checked build
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -294,12 +295,18 @@ enum : uint32_t { ERR_NONE = 0, ERR_TIMEOUT = 1, ERR_BOUNDS = 2 };
 // status word and is false, and the caller skips the access.  In the normal
 // build it is always true and costs nothing.
 #ifdef RB_BOUNDS_CHECK
-__device__ __forceinline__ bool rb_in_bounds(long long i, long long n, uint32_t* status) {
+// The first failure of a launch sequence also prints its source line, index
+// and bound (device printf, flushed at the next host synchronisation).
+__device__ __forceinline__ bool rb_in_bounds(long long i, long long n, uint32_t* status, int line) {
   if (i >= 0 && i < n) return true;
-  if (status) atomicOr(status, ERR_BOUNDS);
+  if (status) {
+    atomicOr(status, ERR_BOUNDS);
+    if (atomicCAS(status + 1, 0u, (uint32_t)line) == 0u)
+      printf("index check failed at line %d: %lld not in [0, %lld)\n", line, i, n);
+  }
   return false;
 }
-#define RB_IN(i, n, status) ::ribo::rb_in_bounds((long long)(i), (long long)(n), (status))
+#define RB_IN(i, n, status) ::ribo::rb_in_bounds((long long)(i), (long long)(n), (status), __LINE__)
 #else
 #define RB_IN(i, n, status) true
 #endif

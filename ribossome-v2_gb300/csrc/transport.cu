@@ -650,10 +650,12 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
       S.base[tid] = make_int2(basex, basey);
       {
         // A dispersing cell sends every mover down the general path, and so
-        // does a displacement of 2^22 cells or more.  Below that a start s
-        // in [0, 1] gives fl(s + d) in [d, d + 1] exactly at the ends, so a
-        // main-path mover's window offset is 1 or 2 per axis (0 or 1 in y
-        // after settling) and its bin needs no clamp.
+        // does a displacement of 2^22 cells or more.  Below that, for a start
+        // s in [0, 1]: d <= fl(s + d) <= fl(d + 1) <= floor(d) + 2 (an
+        // integer, representable), so a main-path mover's window offset
+        // floor(fl(s + d)) - floor(d) + 1 is 1, 2 or 3 per axis -- 3 when d is
+        // just below an integer and s + d rounds up to the next one -- and 0
+        // to 2 in y after settling: its bin is below 16 and needs no clamp.
         const bool general_only = disperse || !(rb_abs(disp.x) < 4194304.0f && rb_abs(disp.y) < 4194304.0f);
         const uint32_t t_hop = st::u24_threshold(p_diff);
         S.thr[tid] = make_uint4(__float_as_uint(p_bound), general_only ? st::ALWAYS : t_hop, t_hop,
@@ -867,7 +869,7 @@ __global__ void __launch_bounds__(st::NT, 4) k_scatter_tiled(const __grid_consta
         float py = (bound ? m0.w : rb_u2f(ru.y)) + m0.y;
         if (z24 < th.w) py -= 1.0f;  // rfz < p_diff + p_settle (and not below p_diff)
         const int2 bs = S.base[ct];
-        const uint32_t bi = (uint32_t)((rb_floor_i(py) - bs.y) * 4 + (rb_floor_i(px) - bs.x));  // in [1, 10]
+        const uint32_t bi = (uint32_t)((rb_floor_i(py) - bs.y) * 4 + (rb_floor_i(px) - bs.x));  // in [1, 15]
         if (RB_IN(bi, 16, d.status)) {
           const uint16_t sl = S.slot[bi][ct];
           if (sl != st::FAR) {
