@@ -543,44 +543,14 @@ __device__ __forceinline__ bool coarse_residual(const CLv& L, int y, int x, floa
   return true;
 }
 
-template <class S, bool MP = false>
-__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ S s, int nu_pre, int nu_post, int coarse) {
-  const CoarsePass& e = coarse_of(s);
+// The V-cycle of a coarse set whose top level (flags, rhs, p) is in shared
+// memory with its codes built: pre-smooth and restrict down to the coarsest
+// level, solve it, prolong and post-smooth back up; the top level's p is
+// left in shared memory.
+template <bool MP>
+__device__ __forceinline__ void coarse_cycle(const CoarsePass& e, unsigned char* smem, int nu_pre, int nu_post,
+                                             int coarse) {
   const CoarseSet& cs = e.cs;
-  const bool TOP = e.top != 0;
-  extern __shared__ __align__(16) unsigned char smem[];
-  // every plane cell starts as non-water, p = rhs = 0 (the rings stay so)
-  {
-    float* f = reinterpret_cast<float*>(smem);
-    for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) f[i] = 0.0f;
-    uint8_t* b = reinterpret_cast<uint8_t*>(f + 2 * cs.total);
-    for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) b[i] = 0;
-  }
-  __syncthreads();
-  {
-    const CLv L = coarse_level(cs, smem, 0);
-    for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
-      const int y = idx / L.nx, x = idx - y * L.nx;
-      uint8_t f;
-      float r, p = 0.0f;
-      if (TOP) {
-        const size_t gi = (size_t)y * e.fw + x;
-        f = e.mask[gi] ? 0 : 1;
-        r = e.div[gi];
-        p = f ? e.pa[gi] : 0.0f;
-      } else {
-        f = cs.fl_top[idx];
-        r = cs.rhs_top[idx];
-      }
-      const int a = L.at(y, x);
-      L.F[a] = f;
-      L.P[a] = f ? p : 0.0f;
-      L.R[a] = f ? r : 0.0f;
-    }
-    __syncthreads();
-    coarse_codes(L);
-    __syncthreads();
-  }
   for (int l = 0; l + 1 < cs.n; l++) {
     const CLv L = coarse_level(cs, smem, l), C = coarse_level(cs, smem, l + 1);
     for (int k = 0; k < nu_pre; k++) {
@@ -648,6 +618,47 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
       coarse_sweep(L, c0 ^ 1);
     }
   }
+}
+
+template <class S, bool MP = false>
+__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ S s, int nu_pre, int nu_post, int coarse) {
+  const CoarsePass& e = coarse_of(s);
+  const CoarseSet& cs = e.cs;
+  const bool TOP = e.top != 0;
+  extern __shared__ __align__(16) unsigned char smem[];
+  // every plane cell starts as non-water, p = rhs = 0 (the rings stay so)
+  {
+    float* f = reinterpret_cast<float*>(smem);
+    for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) f[i] = 0.0f;
+    uint8_t* b = reinterpret_cast<uint8_t*>(f + 2 * cs.total);
+    for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) b[i] = 0;
+  }
+  __syncthreads();
+  {
+    const CLv L = coarse_level(cs, smem, 0);
+    for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
+      const int y = idx / L.nx, x = idx - y * L.nx;
+      uint8_t f;
+      float r, p = 0.0f;
+      if (TOP) {
+        const size_t gi = (size_t)y * e.fw + x;
+        f = e.mask[gi] ? 0 : 1;
+        r = e.div[gi];
+        p = f ? e.pa[gi] : 0.0f;
+      } else {
+        f = cs.fl_top[idx];
+        r = cs.rhs_top[idx];
+      }
+      const int a = L.at(y, x);
+      L.F[a] = f;
+      L.P[a] = f ? p : 0.0f;
+      L.R[a] = f ? r : 0.0f;
+    }
+    __syncthreads();
+    coarse_codes(L);
+    __syncthreads();
+  }
+  coarse_cycle<MP>(e, smem, nu_pre, nu_post, coarse);
   {
     const CLv L = coarse_level(cs, smem, 0);
     for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
@@ -655,6 +666,382 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
       const float v = L.P[L.at(y, x)];
       if (TOP) e.pa[(size_t)y * e.fw + x] = v;
       else cs.p_out[idx] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cluster V-cycle of the latency-bound levels.
+//
+// The small fine levels (the slab levels: at most SLAB_MAX_CELLS owned cells
+// per CTA) and the coarsest level run in ONE launch per V-cycle, on a
+// thread-block cluster of NC CTAs of COARSE_THREADS threads.  CTA r owns rows
+// [r R_l, (r + 1) R_l) of slab level l, with R_l = 2 R_{l+1} (even), so the
+// children of a coarse row are rows of the same CTA: restriction stays inside
+// the CTA.  A CTA holds its rows in a window with G = 2 nu + 1 ghost rows on
+// each side, stored like the coarse levels (colour planes, a non-water column
+// on each side, neighbour codes); the window's first and last rows are never
+// updated.  This is the fine kernels' box argument along y: after s
+// half-sweeps the rows at distance >= s from the window edge hold exactly
+// what one dispatch per half-sweep gives, so after 2 nu half-sweeps the owned
+// rows and their one-row ring are exact, and a level is swept with block
+// barriers only.  Owners push what other windows need through distributed
+// shared memory (remote stores, made visible by the next cluster barrier):
+// the right-hand sides and water flags of the rows they restrict, their
+// pre-smoothed p, and the rows of their post-smoothed p that the finer
+// level's windows prolong from (into a per-level staging area of natural-
+// order rows).  The coarsest slab level restricts into CTA 0's copy of the
+// coarsest level, which CTA 0 solves alone (the coarse kernel's code) while
+// the other CTAs wait at the next cluster barrier.  Cluster barriers are
+// hardware barriers: every CTA executes the same sequence of them, and no
+// thread spins on memory.
+constexpr int MG_MAX_SLAB_LEVELS = 8;
+constexpr int SLAB_MAX_CELLS = 1024;  // owned cells per CTA of a slab level (more: issue-bound on NC SMs)
+struct SlabLv {
+  int nx, ny;
+  int R;       // rows owned per CTA
+  int wr;      // window rows: R + 2 G
+  int qs, pl;  // cells per colour row, cells per colour plane (wr * qs)
+  int off;     // first cell of the window's planes
+  int so;      // first float of the staging area (coarse correction rows)
+  int srows;   // staging rows: R / 2 + G + 1
+  int cnx;     // width of the next coarser level (staging row length)
+  float eps;
+};
+struct ClusterPass {
+  int nslab;  // slab levels, finest first (levels m .. g - 1)
+  SlabLv w[MG_MAX_SLAB_LEVELS];
+  int G;      // ghost rows on each side
+  int par;    // colour of window cell (row 0, padded column 0), the same in every CTA
+  int nc;     // CTAs of the cluster
+  CoarsePass co;  // the coarsest level (g = nl - 1); co.cs.total = cells of every plane
+  // level m's inputs and output: levels >= 1 read rhs and flags and write p;
+  // level 0 reads the wall mask, divergence and pressure_a and writes pressure_a
+  const float* rhs_top;
+  const uint8_t* fl_top;
+  float* p_out;
+  uint32_t* status;  // index checks of the bounds-checked build
+};
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_sync() {
+  cluster_arrive();
+  cluster_wait();
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+// The address of `p` (this CTA's shared memory) in CTA `rank` of the cluster.
+template <class T>
+__device__ __forceinline__ T* cta_map(T* p, uint32_t rank) {
+  uint64_t r;
+  asm volatile("mapa.u64 %0, %1, %2;\n" : "=l"(r) : "l"(reinterpret_cast<uint64_t>(p)), "r"(rank));
+  return reinterpret_cast<T*>(r);
+}
+__device__ __forceinline__ int floor_half(int v) { return v >= 0 ? v / 2 : -((1 - v) / 2); }
+
+// A slab level's window in shared memory (P, R: float; K, F: byte arrays of
+// `total` cells each, like the coarse levels') and its staging area.
+struct Win {
+  SlabLv L;
+  int par;
+  float* P;
+  float* R;
+  uint8_t* K;
+  uint8_t* F;
+  float* S;
+  __device__ __forceinline__ Win(const SlabLv& l, int par_, unsigned char* smem, int total) : L(l), par(par_) {
+    float* base = reinterpret_cast<float*>(smem);
+    P = base + l.off;
+    R = base + total + l.off;
+    uint8_t* bytes = reinterpret_cast<uint8_t*>(base + 2 * total);  // K and F arrays, then the staging floats
+    K = bytes + l.off;
+    F = K + total;
+    S = reinterpret_cast<float*>(bytes + 2 * total) + l.so;
+  }
+  // window row wy, padded column i (level column i - 1)
+  __device__ __forceinline__ int at(int wy, int i) const { return ((i + wy + par) & 1) * L.pl + wy * L.qs + (i >> 1); }
+};
+
+__device__ __forceinline__ void win_codes(const Win& W) {
+  const SlabLv& L = W.L;
+  for (int e = threadIdx.x; e < L.wr * L.nx; e += COARSE_THREADS) {
+    const int wy = e / L.nx, i = e - wy * L.nx + 1;
+    const int a = W.at(wy, i);
+    uint8_t k = 0;
+    if (wy > 0 && wy < L.wr - 1 && W.F[a]) {
+      const int o = i & 1, b = a + (((i + wy + W.par) & 1) ? -L.pl : L.pl);
+      k = (uint8_t)(1 + W.F[b - 1 + o] + W.F[b + o] + W.F[b - L.qs] + W.F[b + L.qs]);
+    }
+    W.K[a] = k;
+  }
+}
+
+// One colour of a red-black sweep over window rows lo..hi (multigrid.wgsl:60-77).
+__device__ __forceinline__ void win_sweep(const Win& W, int lo, int hi, int c) {
+  const SlabLv& L = W.L;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* Pc = W.P + c * L.pl;
+  const float* Po = W.P + (c ^ 1) * L.pl;
+  const float* Rc = W.R + c * L.pl;
+  const uint8_t* Kc = W.K + c * L.pl;
+  for (int j = lo + warp; j <= hi; j += COARSE_THREADS / 32) {
+    const int o = (c + j + W.par) & 1;  // padded column parity of colour c in window row j
+    for (int q = lane + 1 - o; 2 * q + o <= L.nx; q += 32) {
+      const int a = j * L.qs + q;
+      const uint8_t kk = Kc[a];
+      if (!kk) continue;
+      float sum = 0.0f;
+      sum += Po[a - 1 + o];
+      sum += Po[a + o];
+      sum += Po[a - L.qs];
+      sum += Po[a + L.qs];
+      Pc[a] = (sum - Rc[a]) / ((float)(kk - 1) + L.eps);
+    }
+  }
+  __syncthreads();
+}
+
+// Residual of window cell (wy, i) if it is updated (multigrid.wgsl:82-105).
+__device__ __forceinline__ bool win_residual(const Win& W, int wy, int i, float& res) {
+  const SlabLv& L = W.L;
+  const int a = W.at(wy, i);
+  const uint8_t kk = W.K[a];
+  if (!kk) return false;
+  const int o = i & 1, b = a + (((i + wy + W.par) & 1) ? -L.pl : L.pl);
+  float s = 0.0f;
+  s += W.P[b - 1 + o];
+  s += W.P[b + o];
+  s += W.P[b - L.qs];
+  s += W.P[b + L.qs];
+  res = W.R[a] - (s - ((float)(kk - 1) + L.eps) * W.P[a]);
+  return true;
+}
+
+// Pushes this CTA's owned rows of `a1` (and of `a2`, an array of the same
+// layout, when given: window arrays of floats or bytes, both colour planes)
+// into the windows of the other CTAs that hold them as ghost rows.  Each
+// thread takes an owned element and stores it to those CTAs: CTA rr's window
+// holds rows [rr R - G, rr R + R + G).
+template <class T1, class T2>
+__device__ __forceinline__ void win_push_owned(const Win& W, T1* a1, T2* a2, int G, int nc, uint32_t rank,
+                                               uint32_t* status) {
+  const SlabLv& L = W.L;
+  const int r0 = (int)rank * L.R;
+  const int y1 = r0 + L.R < L.ny ? r0 + L.R : L.ny;
+  const int n = (y1 - r0) * 2 * L.qs;
+  for (int e = threadIdx.x; e < n; e += COARSE_THREADS) {
+    const int q = e % L.qs, t = e / L.qs, plane = t & 1, y = r0 + (t >> 1);
+    const int a = plane * L.pl + (y - r0 + G) * L.qs + q;
+    const T1 v1 = a1[a];
+    const T2 v2 = a2 ? a2[a] : T2(0);
+    int rlo = y - G - L.R + 1;
+    rlo = rlo <= 0 ? 0 : (rlo + L.R - 1) / L.R;
+    int rhi = (y + G) / L.R;
+    if (rhi > nc - 1) rhi = nc - 1;
+    for (int rr = rlo; rr <= rhi; rr++) {
+      if (rr == (int)rank) continue;
+      const int d = a + (r0 - rr * L.R) * L.qs;
+      if (!RB_IN(d, 2 * L.pl, status)) continue;
+      *cta_map(a1 + d, (uint32_t)rr) = v1;
+      if (a2) *cta_map(a2 + d, (uint32_t)rr) = v2;
+    }
+  }
+}
+
+// Pushes rows [c0, c1) of a coarse level's p (read by `get(cy, cx)`) into the
+// staging areas of slab level W (the next finer one) of the CTAs whose
+// windows prolong from them: CTA rr's window rows [rr R - G, rr R + R + G)
+// read coarse rows floor(y / 2), staged from row floor((rr R - G) / 2) on.
+template <class Get>
+__device__ __forceinline__ void stage_push(const Win& W, int c0, int c1, int G, int nc, uint32_t* status, Get&& get) {
+  const SlabLv& L = W.L;
+  const int n = (c1 - c0) * L.cnx;
+  for (int e = threadIdx.x; e < n; e += COARSE_THREADS) {
+    const int cy = c0 + e / L.cnx, cx = e % L.cnx;
+    const float v = get(cy, cx);
+    int rlo = 2 * cy - L.R - G + 1;
+    rlo = rlo <= 0 ? 0 : (rlo + L.R - 1) / L.R;
+    int rhi = (2 * cy + 1 + G) / L.R;
+    if (rhi > nc - 1) rhi = nc - 1;
+    for (int rr = rlo; rr <= rhi; rr++) {
+      const int row = cy - floor_half(rr * L.R - G);
+      if (row < 0 || row >= L.srows) continue;
+      const int si = row * L.cnx + cx;
+      if (RB_IN(si, L.srows * L.cnx, status)) *cta_map(W.S + si, (uint32_t)rr) = v;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(COARSE_THREADS, 1)
+    k_mg_cluster(const __grid_constant__ ClusterPass cp, int nu_pre, int nu_post, int coarse) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t rank = cluster_rank();
+  const CoarsePass& e = cp.co;
+  const CoarseSet& cs = e.cs;
+  const int total = cs.total, G = cp.G, nc = cp.nc;
+  // every cell starts as non-water, p = rhs = 0 (rings, rows outside the level)
+  {
+    float4* f = reinterpret_cast<float4*>(smem);
+    const int n16 = (10 * total + 15) / 16;
+    for (int i = threadIdx.x; i < n16; i += COARSE_THREADS) f[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  __syncthreads();
+  cluster_arrive();  // every CTA has started and cleared its memory (waited for before the first remote access)
+  // the top slab level: the whole window from global memory
+  {
+    const Win W(cp.w[0], cp.par, smem, total);
+    const SlabLv& L = W.L;
+    const int r0 = (int)rank * L.R, n = L.wr * L.nx;
+    const bool TOP = e.top != 0;
+    constexpr int BATCH = 4;
+    for (int e0 = threadIdx.x; e0 < n; e0 += BATCH * COARSE_THREADS) {
+      uint8_t f[BATCH];
+      float r[BATCH], p[BATCH];
+#pragma unroll
+      for (int u = 0; u < BATCH; u++) {  // a batch's loads are all issued before its stores
+        const int el = e0 + u * COARSE_THREADS;
+        const int wy = el / L.nx, x = el - wy * L.nx, y = r0 - G + wy;
+        const bool in = el < n && y >= 0 && y < L.ny;
+        const size_t gi = in ? (size_t)y * (TOP ? e.fw : L.nx) + x : 0;
+        if (TOP) {
+          f[u] = in && !e.mask[gi] ? 1 : 0;
+          r[u] = e.div[gi];
+          p[u] = e.pa[gi];
+        } else {
+          f[u] = in ? cp.fl_top[gi] : 0;
+          r[u] = cp.rhs_top[gi];
+          p[u] = 0.0f;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < BATCH; u++) {
+        const int el = e0 + u * COARSE_THREADS;
+        if (el >= n) continue;
+        const int wy = el / L.nx, i = el - wy * L.nx + 1;
+        const int a = W.at(wy, i);
+        W.F[a] = f[u];
+        W.P[a] = f[u] ? p[u] : 0.0f;
+        W.R[a] = f[u] ? r[u] : 0.0f;
+      }
+    }
+    __syncthreads();
+  }
+  // pre-smooth, residual and restriction down the slab levels
+  for (int s = 0; s < cp.nslab; s++) {
+    const Win W(cp.w[s], cp.par, smem, total);
+    const SlabLv& L = W.L;
+    const int r0 = (int)rank * L.R;
+    win_codes(W);
+    __syncthreads();
+    const int lo = max(1, G - r0), hi = min(L.wr - 2, G - r0 + L.ny - 1);
+    for (int k = 0; k < nu_pre; k++) {
+      win_sweep(W, lo, hi, 0);
+      win_sweep(W, lo, hi, 1);
+    }
+    // restriction of the owned rows into the next slab level's owned rows
+    // (local, then pushed to the windows that hold them as ghost rows) or
+    // into CTA 0's coarsest level (remote)
+    const bool last = s + 1 == cp.nslab;
+    const CLv T = coarse_level(cs, smem, 0);
+    const int cnx = last ? cs.nx[0] : cp.w[s + 1].nx, cny = last ? cs.ny[0] : cp.w[s + 1].ny, cR = L.R / 2;
+    const Win C(cp.w[last ? s : s + 1], cp.par, smem, total);
+    float* tP = cta_map(T.P, 0u);
+    float* tR = cta_map(T.R, 0u);
+    uint8_t* tF = cta_map(T.F, 0u);
+    if (s == 0) cluster_wait();
+    const int c0 = (int)rank * cR;
+    for (int ce = threadIdx.x; ce < cR * cnx; ce += COARSE_THREADS) {
+      const int cyl = ce / cnx, cx = ce - cyl * cnx, cy = c0 + cyl;
+      if (cy >= cny) continue;
+      float sum = 0.0f;
+      uint32_t nf = 0;
+      for (uint32_t q = 0; q < 4; q++) {
+        float res;
+        const int fy = cy * 2 + (int)(q >> 1), fx = cx * 2 + (int)(q & 1u);
+        if (!win_residual(W, fy - r0 + G, fx + 1, res)) continue;
+        sum += res;
+        nf++;
+      }
+      const uint8_t fl = nf > 0u ? 1 : 0;
+      const float rh = nf > 0u ? 2.0f * sum / (float)(nf > 1u ? nf : 1u) : 0.0f;
+      if (last) {
+        const int a = T.at(cy, cx);
+        tF[a] = fl;
+        tR[a] = rh;
+        tP[a] = 0.0f;
+      } else {
+        const int a = C.at(cyl + G, cx + 1);
+        C.F[a] = fl;
+        C.R[a] = rh;
+      }
+    }
+    if (!last) {
+      __syncthreads();
+      win_push_owned(C, C.R, C.F, G, nc, rank, cp.status);
+    }
+    cluster_sync();  // the next level's windows (or the coarsest level) are complete everywhere
+  }
+  // every CTA's windows are pre-smoothed: push the owned p to the windows
+  // that hold it as ghost rows (nobody writes a window's p until the next
+  // barrier); CTA 0 solves the coarsest level and stages it for the
+  // coarsest slab level
+  for (int s = 0; s < cp.nslab; s++) {
+    const Win W(cp.w[s], cp.par, smem, total);
+    win_push_owned(W, W.P, (uint8_t*)nullptr, G, nc, rank, cp.status);
+  }
+  if (rank == 0) {
+    const CLv T = coarse_level(cs, smem, 0);
+    coarse_codes(T);
+    __syncthreads();
+    coarse_cycle<false>(e, smem, nu_pre, nu_post, coarse);
+    const Win W(cp.w[cp.nslab - 1], cp.par, smem, total);
+    stage_push(W, 0, T.ny, G, nc, cp.status, [&](int cy, int cx) { return T.P[T.at(cy, cx)]; });
+  }
+  cluster_sync();  // ghost p and the coarse correction have arrived
+  // prolongation (from the staged coarse rows) and post-smooth up the slab levels
+  for (int s = cp.nslab - 1; s >= 0; s--) {
+    const Win W(cp.w[s], cp.par, smem, total);
+    const SlabLv& L = W.L;
+    const int r0 = (int)rank * L.R, sb = floor_half(r0 - G);
+    for (int el = threadIdx.x; el < L.wr * L.nx; el += COARSE_THREADS) {
+      const int wy = el / L.nx, x = el - wy * L.nx, y = r0 - G + wy;
+      if (y < 0 || y >= L.ny) continue;
+      const int a = W.at(wy, x + 1);
+      if (!W.F[a]) continue;
+      const int si = (floor_half(y) - sb) * L.cnx + x / 2;
+      if (RB_IN(si, L.srows * L.cnx, cp.status)) W.P[a] += W.S[si];
+    }
+    __syncthreads();
+    const int lo = max(1, G - r0), hi = min(L.wr - 2, G - r0 + L.ny - 1);
+    for (int k = 0; k < nu_post; k++) {
+      win_sweep(W, lo, hi, 0);
+      win_sweep(W, lo, hi, 1);
+    }
+    if (s > 0) {
+      // the owned rows are final: stage them for the next finer level
+      const Win F(cp.w[s - 1], cp.par, smem, total);
+      int c1 = r0 + L.R;
+      if (c1 > L.ny) c1 = L.ny;
+      stage_push(F, r0, c1, G, nc, cp.status, [&](int cy, int cx) { return W.P[W.at(cy - r0 + G, cx + 1)]; });
+      cluster_sync();
+    }
+  }
+  // the top slab level's owned rows leave for the next finer level (or pressure_a)
+  {
+    const Win W(cp.w[0], cp.par, smem, total);
+    const SlabLv& L = W.L;
+    const int r0 = (int)rank * L.R;
+    const bool TOP = e.top != 0;
+    for (int el = threadIdx.x; el < L.R * L.nx; el += COARSE_THREADS) {
+      const int yl = el / L.nx, x = el - yl * L.nx, y = r0 + yl;
+      if (y >= L.ny) continue;
+      const float v = W.P[W.at(yl + G, x + 1)];
+      if (TOP) e.pa[(size_t)y * e.fw + x] = v;
+      else cp.p_out[(size_t)y * L.nx + x] = v;
     }
   }
 }
@@ -830,13 +1217,172 @@ static void launch_post(const Dev& d, const MgLevel* levels, int l, const MgBufs
   RB_LAUNCH(name, bytes, s, k_mg_post<B, MgOne><<<grid, blk, B::SMEM, s>>>(one, c.post));
 }
 
+// CTAs per cluster that k_mg_cluster can run with on this device at the
+// largest opt-in shared memory (16, else 8; 0: no cluster launch).  Queried
+// once per device outside stream capture; a call during capture before the
+// first query answers 0 (the launch-per-level path, same results).
+static int cluster_ctas(cudaStream_t s) {
+  static std::atomic<int> cache[64];
+  const int dev = DeviceOnce::device();
+  const int v = cache[dev].load(std::memory_order_acquire);
+  if (v != 0) return v < 0 ? 0 : v;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return 0;
+  }
+  int smax = 0, found = -1;
+  if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess && smax > 0 &&
+      cudaFuncSetAttribute(k_mg_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) == cudaSuccess &&
+      cudaFuncSetAttribute(k_mg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    for (int nc : {16, 8}) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)nc;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)nc);
+      cfg.blockDim = dim3(COARSE_THREADS);
+      cfg.dynamicSmemBytes = (size_t)smax;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, k_mg_cluster, &cfg) == cudaSuccess && n >= 1) {
+        found = nc;
+        break;
+      }
+    }
+  }
+  cudaGetLastError();
+  cache[dev].store(found, std::memory_order_release);
+  return found < 0 ? 0 : found;
+}
+
+static int smem_optin() {
+  static std::atomic<int> cache[64];
+  const int dev = DeviceOnce::device();
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      return 0;
+    }
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+
+// The cluster V-cycle's arguments for a world: the coarsest level g and the
+// slab levels m .. g - 1 above it with at most SLAB_MAX_CELLS owned cells per
+// CTA, as far up as their windows fit in one CTA's shared memory.  False
+// when no slab level qualifies.
+static bool cluster_pass(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MgConfig& c, int nc,
+                         size_t smax, ClusterPass* out, int* m_out, size_t* smem_out) {
+  const int g = nl - 1;
+  if (nc <= 0 || g < 1 || multigrid_first_coarse_level(levels, nl) >= nl) return false;
+  const int G = 2 * (c.pre > c.post ? c.pre : c.post) + 1;
+  const int Rk = (levels[g].ny + nc - 1) / nc;
+  const size_t coarse = (size_t)coarse_cells(levels[g].nx, levels[g].ny);
+  size_t win = 0, stage = 0;
+  int m = g;
+  while (m > 0 && g - (m - 1) <= MG_MAX_SLAB_LEVELS) {
+    const MgLevel& L = levels[m - 1];
+    const long R = (long)Rk << (g - (m - 1));
+    if (R * L.nx > SLAB_MAX_CELLS) break;
+    const size_t cells = (size_t)2 * (size_t)(R + 2 * G) * (size_t)coarse_qs(L.nx);
+    const size_t st = (size_t)(R / 2 + G + 1) * (size_t)levels[m].nx;
+    if (10 * (win + cells + coarse) + 4 * (stage + st) + 16 > smax) break;
+    win += cells;
+    stage += st;
+    m--;
+  }
+  if (m == g) return false;
+  ClusterPass& cp = *out;
+  cp = ClusterPass{};
+  cp.nslab = g - m;
+  cp.G = G;
+  cp.par = (G + 1) & 1;
+  cp.nc = nc;
+  int off = 0, so = 0;
+  for (int l = m; l < g; l++) {
+    SlabLv& w = cp.w[l - m];
+    w.nx = levels[l].nx;
+    w.ny = levels[l].ny;
+    w.R = Rk << (g - l);
+    w.wr = w.R + 2 * G;
+    w.qs = coarse_qs(w.nx);
+    w.pl = w.wr * w.qs;
+    w.off = off;
+    w.so = so;
+    w.srows = w.R / 2 + G + 1;
+    w.cnx = levels[l + 1].nx;
+    w.eps = levels[l].eps;
+    off += 2 * w.pl;
+    so += w.srows * w.cnx;
+  }
+  CoarseSet& cs = cp.co.cs;
+  cs.n = 1;
+  cs.nx[0] = levels[g].nx;
+  cs.ny[0] = levels[g].ny;
+  cs.eps[0] = levels[g].eps;
+  cs.off[0] = off;
+  off += coarse_cells(levels[g].nx, levels[g].ny);
+  cs.total = off;
+  cp.co.mask = d.mask;
+  cp.co.div = d.div;
+  cp.co.pa = d.pa;
+  cp.co.fw = d.fw;
+  cp.co.top = m == 0 ? 1 : 0;
+  cp.rhs_top = b.rhs + levels[m].off;
+  cp.fl_top = b.fluid + levels[m].off;
+  cp.p_out = b.p + levels[m].off;
+  cp.status = d.status;
+  *m_out = m;
+  *smem_out = ((size_t)10 * off + (size_t)4 * so + 15) & ~(size_t)15;
+  return true;
+}
+
 void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const MgBufs& b, const MgConfig& c, cudaStream_t s) {
   set_smem_attrs();
+  const int cycles = c.cycles < 1 ? 1 : c.cycles;
+  {
+    const int nc = cluster_ctas(s);
+    ClusterPass cp;
+    int m = 0;
+    size_t smem = 0;
+    if (cluster_pass(d, levels, nl, b, c, nc, (size_t)smem_optin(), &cp, &m, &smem)) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)nc;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)nc);
+      cfg.blockDim = dim3(COARSE_THREADS);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = s;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      const double bytes = (m == 0 ? 13.0 : 9.0) * (double)levels[m].nx * levels[m].ny;
+      for (int cy = 0; cy < cycles; cy++) {
+        for (int l = 0; l < m; l++) {
+          if (small_tiles(levels[l], c)) launch_pre<BoxSmall>(d, levels, l, b, c, s);
+          else launch_pre<BoxBig>(d, levels, l, b, c, s);
+        }
+        RB_LAUNCH("mg_cluster_vcycle", bytes, s, cudaLaunchKernelEx(&cfg, k_mg_cluster, cp, c.pre, c.post, c.coarse));
+        for (int l = m - 1; l >= 0; l--) {
+          if (small_tiles(levels[l], c)) launch_post<BoxSmall>(d, levels, l, b, c, s);
+          else launch_post<BoxBig>(d, levels, l, b, c, s);
+        }
+      }
+      return;
+    }
+  }
   const int k = multigrid_first_coarse_level(levels, nl);
   size_t coarse_smem = 0;
   double coarse_bytes = 0.0;
   const CoarseOne co{coarse_pass(d, levels, nl, b, &coarse_smem, &coarse_bytes)};
-  const int cycles = c.cycles < 1 ? 1 : c.cycles;
   for (int cy = 0; cy < cycles; cy++) {
     for (int l = 0; l < k; l++) {
       if (small_tiles(levels[l], c)) launch_pre<BoxSmall>(d, levels, l, b, c, s);
