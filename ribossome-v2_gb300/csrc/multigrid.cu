@@ -9,6 +9,7 @@
 #include <cuda_fp16.h>
 #include <string.h>
 
+#include <type_traits>
 #include <vector>
 
 #include "ribo_dev.cuh"
@@ -106,6 +107,25 @@ __global__ void k_mg_finish(const __grid_constant__ Dev d, Lv L) {
   d.pa[(size_t)y * d.fw + x] = L.p[(size_t)y * L.nx + x];
 }
 
+// Neighbour codes of level L (0: not water, else 1 + the water neighbours
+// inside the level, multigrid.wgsl:29-45) and, when C is given, the water
+// flags of the next coarser level: a coarse cell is water when any of its four
+// children is (the restriction's nf > 0, multigrid.wgsl:82-105).  The flags
+// follow the wall mask alone, so they and the codes are built once per mask.
+__global__ void k_mg_codes(Lv L, uint8_t* __restrict__ code, uint8_t* __restrict__ cfl, int cnx, int cny) {
+  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  if (x >= L.nx || y >= L.ny) return;
+  const size_t i = (size_t)y * L.nx + x;
+  const uint8_t* fl = L.fl;
+  uint8_t k = 0;
+  if (fl[i])
+    k = (uint8_t)(1 + (x > 0 && fl[i - 1]) + (x + 1 < L.nx && fl[i + 1]) + (y > 0 && fl[i - L.nx]) +
+                  (y + 1 < L.ny && fl[i + L.nx]));
+  code[i] = k;
+  if (cfl && !(x & 1) && !(y & 1) && x / 2 < cnx && y / 2 < cny)
+    cfl[(size_t)(y / 2) * cnx + x / 2] = (fl[i] | fl[i + 1] | fl[i + L.nx] | fl[i + L.nx + 1]) ? 1 : 0;
+}
+
 // fluid.wgsl:553-608: one Jacobi sweep pin -> pout; cells outside the grid
 // count as walls (p = 0, solid), wall neighbours mirror p_c.
 __global__ void k_jacobi(const __grid_constant__ Dev d, const float* __restrict__ pin, float* __restrict__ pout) {
@@ -183,6 +203,7 @@ struct RbBox {
   // p and rhs (float, both colours), neighbour codes (both colours), water
   // flags (natural order, used to build the codes)
   static constexpr size_t SMEM = (size_t)2 * PL * 4 * 2 + (size_t)2 * PL + (size_t)RH * W;
+  static constexpr size_t SMEM_CODED = (size_t)2 * PL * 4 * 2 + (size_t)2 * PL;  // no flag array (codes loaded)
   __host__ __device__ static constexpr int tile_w(int H) { return W - 2 * H; }
   __host__ __device__ static constexpr int tile_h(int H) { return RH - 2 * H; }
   __host__ __device__ static constexpr bool fits(int H) { return tile_w(H) >= 2 && tile_h(H) >= 2; }
@@ -224,7 +245,10 @@ __device__ __forceinline__ float rb_nb_sum(const RbSmem<B>& S, int j, int i, int
 // water flag, rhs and initial p of a cell (gi = its index, 0 outside the
 // level); then builds the neighbour codes.  Loads are issued for every cell
 // (index 0 outside the level) so they overlap.
-template <class B, class Fn>
+// With CODED the cell's byte is its neighbour code (precomputed per level,
+// 0: not water): the box edge is forced to 0 (never updated) and no code
+// pass runs.
+template <class B, bool CODED = false, class Fn>
 __device__ __forceinline__ void rb_load(const RbSmem<B>& S, int X0, int Y0, int nx, int ny, Fn&& cell) {
   const int tid = threadIdx.y * BX + threadIdx.x;
   constexpr int N = B::W * B::RH, NT = BX * BY, IT = (N + NT - 1) / NT, BATCH = 4;
@@ -247,20 +271,23 @@ __device__ __forceinline__ void rb_load(const RbSmem<B>& S, int X0, int Y0, int 
       if (it0 + u >= IT || e >= N) continue;
       const int j = e / B::W, i = e - j * B::W;
       const int a = S.at(j, i);
-      S.F[e] = f[u];
+      if constexpr (CODED) S.K[a] = (i == 0 || j == 0 || i == B::W - 1 || j == B::RH - 1) ? 0 : f[u];
+      else S.F[e] = f[u];
       S.P[a] = f[u] ? p[u] : 0.0f;
       S.R[a] = f[u] ? r[u] : 0.0f;
     }
   }
   __syncthreads();
-  for (int e = tid; e < B::W * B::RH; e += BX * BY) {
-    const int j = e / B::W, i = e - j * B::W;
-    uint8_t k = 0;
-    if (i > 0 && j > 0 && i < B::W - 1 && j < B::RH - 1 && S.F[e])
-      k = (uint8_t)(1 + S.F[e - 1] + S.F[e + 1] + S.F[e - B::W] + S.F[e + B::W]);
-    S.K[S.at(j, i)] = k;
+  if constexpr (!CODED) {
+    for (int e = tid; e < B::W * B::RH; e += BX * BY) {
+      const int j = e / B::W, i = e - j * B::W;
+      uint8_t k = 0;
+      if (i > 0 && j > 0 && i < B::W - 1 && j < B::RH - 1 && S.F[e])
+        k = (uint8_t)(1 + S.F[e - 1] + S.F[e + 1] + S.F[e - B::W] + S.F[e + B::W]);
+      S.K[S.at(j, i)] = k;
+    }
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 // nsweeps half-sweeps over the cells at distance >= 1 from the box edge;
@@ -312,6 +339,7 @@ struct MgPass {
   const float* r_src;    // right-hand side of the level
   const uint8_t* f_src;  // water flags of the level
   float* p_out;          // smoothed p of the level
+  const uint8_t* k_src;  // neighbour codes of the level (null: built from the flags)
 };
 // A launch over one world's level, or over the same level index of a batch
 // of worlds (the CTA finds its world as the per-cell passes do).
@@ -349,8 +377,14 @@ __device__ __forceinline__ void rb_store_tile(const RbSmem<B>& S, int H, int x0,
 }
 
 // Pre-smooth (nu sweeps) + residual + restrict (multigrid.wgsl:60-105).
-template <class B, bool TOP, class S>
-__global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ S s, int nu) {
+// Coded boxes need no flag array: seven fit in an SM's shared memory, and a
+// single world's kernels fit seven CTAs' registers (32 per thread) without
+// spilling in the sweeps; the batched kernels (member lookup) are held to six.
+template <class S>
+constexpr int mg_min_blocks(bool coded) { return coded ? (std::is_same<S, MgOne>::value ? 7 : 6) : 1; }
+
+template <class B, bool TOP, class S, bool CODED>
+__global__ void __launch_bounds__(BX* BY, mg_min_blocks<S>(CODED)) k_mg_pre(const __grid_constant__ S s, int nu) {
   MgPass e;
   int tile_x, tile_y;
   mg_locate(s, e, tile_x, tile_y);
@@ -363,11 +397,15 @@ __global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ S s, 
   const float* __restrict__ p_src = e.p_src;
   const float* __restrict__ r_src = e.r_src;
   const uint8_t* __restrict__ f_src = e.f_src;
-  rb_load<B>(Sm, x0 - H, y0 - H, L.nx, L.ny, [&](bool in, size_t gi, int, int, uint8_t& f, float& r, float& p) {
-    f = in ? f_src[gi] : 0;
-    r = r_src[gi];
-    p = TOP ? p_src[gi] : 0.0f;  // mg_init: p = water ? pressure_a : 0 (levels >= 1 start at 0)
-  });
+  const uint8_t* __restrict__ k_src = e.k_src;
+  auto cell = [&](const uint8_t* __restrict__ src) {
+    return [&, src](bool in, size_t gi, int, int, uint8_t& f, float& r, float& p) {
+      f = in ? src[gi] : 0;
+      r = r_src[gi];
+      p = TOP ? p_src[gi] : 0.0f;  // mg_init: p = water ? pressure_a : 0 (levels >= 1 start at 0)
+    };
+  };
+  rb_load<B, CODED>(Sm, x0 - H, y0 - H, L.nx, L.ny, cell(CODED ? k_src : f_src));
   rb_sweeps<B>(2 * nu, 0, L.eps, Sm);
   float* __restrict__ p_out = e.p_out;
   rb_store_tile<B>(Sm, H, x0, y0, L.nx, L.ny, [&](size_t i, float v) { p_out[i] = v; });
@@ -393,8 +431,8 @@ __global__ void __launch_bounds__(BX* BY) k_mg_pre(const __grid_constant__ S s, 
 
 // Prolong (add the coarse correction to water cells) + post-smooth nu sweeps
 // (multigrid.wgsl:108-114, 60-77).
-template <class B, class S>
-__global__ void __launch_bounds__(BX* BY) k_mg_post(const __grid_constant__ S s, int nu) {
+template <class B, class S, bool CODED>
+__global__ void __launch_bounds__(BX* BY, mg_min_blocks<S>(CODED)) k_mg_post(const __grid_constant__ S s, int nu) {
   MgPass e;
   int tile_x, tile_y;
   mg_locate(s, e, tile_x, tile_y);
@@ -409,11 +447,15 @@ __global__ void __launch_bounds__(BX* BY) k_mg_post(const __grid_constant__ S s,
   const uint8_t* __restrict__ f_src = e.f_src;
   const float* __restrict__ cp = C.p;
   const int cnx = C.nx;
-  rb_load<B>(Sm, x0 - H, y0 - H, L.nx, L.ny, [&](bool in, size_t gi, int gx, int gy, uint8_t& f, float& r, float& p) {
-    f = in ? f_src[gi] : 0;
-    r = r_src[gi];
-    p = p_src[gi] + cp[in ? (size_t)(gy / 2) * cnx + gx / 2 : 0];
-  });
+  const uint8_t* __restrict__ k_src = e.k_src;
+  auto cell = [&](const uint8_t* __restrict__ src) {
+    return [&, src](bool in, size_t gi, int gx, int gy, uint8_t& f, float& r, float& p) {
+      f = in ? src[gi] : 0;
+      r = r_src[gi];
+      p = p_src[gi] + cp[in ? (size_t)(gy / 2) * cnx + gx / 2 : 0];
+    };
+  };
+  rb_load<B, CODED>(Sm, x0 - H, y0 - H, L.nx, L.ny, cell(CODED ? k_src : f_src));
   rb_sweeps<B>(2 * nu, 0, L.eps, Sm);
   float* __restrict__ p_out = e.p_out;
   rb_store_tile<B>(Sm, H, x0, y0, L.nx, L.ny, [&](size_t i, float v) { p_out[i] = v; });
@@ -1077,6 +1119,19 @@ void launch_multigrid(const Dev& d, const MgLevel* levels, int nl, const MgBufs&
   RB_LAUNCH("mg_finish", 8.0 * cells(L0), s, k_mg_finish<<<grid2(L0.nx, L0.ny), blk, 0, s>>>(d, L0));
 }
 
+void launch_mg_codes(const MgLevel* levels, int nl, const MgBufs& b, cudaStream_t s) {
+  if (!b.code) return;
+  const dim3 blk(BX, BY);
+  for (int l = 0; l < nl; l++) {
+    const Lv L = lv(levels[l], b);
+    const bool down = l + 1 < nl;
+    uint8_t* cfl = down ? b.fluid + levels[l + 1].off : nullptr;
+    const int cnx = down ? levels[l + 1].nx : 0, cny = down ? levels[l + 1].ny : 0;
+    RB_LAUNCH("mg_codes", 2.0 * cells(L), s,
+              k_mg_codes<<<grid2(L.nx, L.ny), blk, 0, s>>>(L, b.code + levels[l].off, cfl, cnx, cny));
+  }
+}
+
 void launch_jacobi(const Dev& d, int iters, cudaStream_t s) {
   const dim3 blk(BX, BY);
   double b = 13.0 * (double)d.fw * d.fh;
@@ -1154,11 +1209,13 @@ static void set_smem_attrs() {
 // pressure_a; the pre-smoothed p goes to p_tmp (level 0) or p2.
 static MgPass pre_pass(const Dev& d, const MgLevel* levels, int l, const MgBufs& b) {
   const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
-  return MgPass{L, C, l == 0 ? d.pa : nullptr, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? b.p_tmp : b.p2 + levels[l].off};
+  return MgPass{L, C, l == 0 ? d.pa : nullptr, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? b.p_tmp : b.p2 + levels[l].off,
+                b.code ? b.code + levels[l].off : nullptr};
 }
 static MgPass post_pass(const Dev& d, const MgLevel* levels, int l, const MgBufs& b) {
   const Lv L = lv(levels[l], b), C = lv(levels[l + 1], b);
-  return MgPass{L, C, l == 0 ? b.p_tmp : b.p2 + levels[l].off, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? d.pa : L.p};
+  return MgPass{L, C, l == 0 ? b.p_tmp : b.p2 + levels[l].off, l == 0 ? d.div : L.rhs, L.fl, l == 0 ? d.pa : L.p,
+                b.code ? b.code + levels[l].off : nullptr};
 }
 static double pre_bytes(const MgLevel* levels, int l) {
   return (l == 0 ? 13.0 : 9.0) * (double)levels[l].nx * levels[l].ny + 5.0 * (double)levels[l + 1].nx * levels[l + 1].ny;
@@ -1203,8 +1260,13 @@ static void launch_pre(const Dev& d, const MgLevel* levels, int l, const MgBufs&
   const dim3 grid(t.nbx, t.nby), blk(BX, BY);
   const char* name = PRE_NAMES[l < 7 ? l : 7];
   const double bytes = pre_bytes(levels, l);
-  if (l == 0) RB_LAUNCH(name, bytes, s, k_mg_pre<B, true, MgOne><<<grid, blk, B::SMEM, s>>>(one, c.pre));
-  else RB_LAUNCH(name, bytes, s, k_mg_pre<B, false, MgOne><<<grid, blk, B::SMEM, s>>>(one, c.pre));
+  if (b.code) {
+    if (l == 0) RB_LAUNCH(name, bytes, s, k_mg_pre<B, true, MgOne, true><<<grid, blk, B::SMEM_CODED, s>>>(one, c.pre));
+    else RB_LAUNCH(name, bytes, s, k_mg_pre<B, false, MgOne, true><<<grid, blk, B::SMEM_CODED, s>>>(one, c.pre));
+  } else {
+    if (l == 0) RB_LAUNCH(name, bytes, s, k_mg_pre<B, true, MgOne, false><<<grid, blk, B::SMEM, s>>>(one, c.pre));
+    else RB_LAUNCH(name, bytes, s, k_mg_pre<B, false, MgOne, false><<<grid, blk, B::SMEM, s>>>(one, c.pre));
+  }
 }
 
 template <class B>
@@ -1214,7 +1276,8 @@ static void launch_post(const Dev& d, const MgLevel* levels, int l, const MgBufs
   const dim3 grid(t.nbx, t.nby), blk(BX, BY);
   const double bytes = post_bytes(levels, l);
   const char* name = POST_NAMES[l < 7 ? l : 7];
-  RB_LAUNCH(name, bytes, s, k_mg_post<B, MgOne><<<grid, blk, B::SMEM, s>>>(one, c.post));
+  if (b.code) RB_LAUNCH(name, bytes, s, k_mg_post<B, MgOne, true><<<grid, blk, B::SMEM_CODED, s>>>(one, c.post));
+  else RB_LAUNCH(name, bytes, s, k_mg_post<B, MgOne, false><<<grid, blk, B::SMEM, s>>>(one, c.post));
 }
 
 // CTAs per cluster that k_mg_cluster can run with on this device at the
@@ -1411,6 +1474,7 @@ struct MgBatchPlan {
   struct Group {
     int level;   // fine level index
     bool small;  // BoxSmall (else BoxBig)
+    bool coded;  // every member loads precomputed neighbour codes (no flag array in the box)
     int n;
     const MgPass* pre;  // device [n]
     const MgPass* post;
@@ -1456,6 +1520,7 @@ MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, c
       std::vector<MgPass> pre, post;
       std::vector<int> start_pre(1, 0), start_post(1, 0), nbx_pre, nbx_post;
       double bpre = 0.0, bpost = 0.0;
+      bool coded = true;
       for (int w = 0; w < n; w++) {
         const MgWorld& W = ws[w];
         if (l >= multigrid_first_coarse_level(W.levels, W.nlevels)) continue;
@@ -1465,6 +1530,7 @@ MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, c
         const TileGrid tp = tile_grid(W.levels[l], sm, 2 * c.pre + 1), tq = tile_grid(W.levels[l], sm, 2 * c.post);
         pre.push_back(pre_pass(W.d, W.levels, l, W.b));
         post.push_back(post_pass(W.d, W.levels, l, W.b));
+        coded = coded && W.b.code != nullptr;
         nbx_pre.push_back(tp.nbx);
         nbx_post.push_back(tq.nbx);
         start_pre.push_back(start_pre.back() + tp.nbx * tp.nby);
@@ -1476,6 +1542,7 @@ MgBatchPlan* multigrid_batch_plan(const MgWorld* ws, int n, const MgConfig& c, c
       MgBatchPlan::Group g{};
       g.level = l;
       g.small = small != 0;
+      g.coded = coded;
       g.n = (int)pre.size();
       g.total_pre = start_pre.back();
       g.total_post = start_post.back();
@@ -1536,10 +1603,18 @@ template <class B>
 static void launch_group_pre_b(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
   const MgSet set{g.pre, g.start_pre, g.nbx_pre, g.n};
   const char* name = PRE_NAMES[g.level < 7 ? g.level : 7];
-  if (g.level == 0)
-    RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, true, MgSet><<<g.total_pre, dim3(BX, BY), B::SMEM, s>>>(set, c.pre));
-  else
-    RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, false, MgSet><<<g.total_pre, dim3(BX, BY), B::SMEM, s>>>(set, c.pre));
+  const dim3 blk(BX, BY);
+  if (g.coded) {
+    if (g.level == 0)
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, true, MgSet, true><<<g.total_pre, blk, B::SMEM_CODED, s>>>(set, c.pre));
+    else
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, false, MgSet, true><<<g.total_pre, blk, B::SMEM_CODED, s>>>(set, c.pre));
+  } else {
+    if (g.level == 0)
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, true, MgSet, false><<<g.total_pre, blk, B::SMEM, s>>>(set, c.pre));
+    else
+      RB_LAUNCH(name, g.bytes_pre, s, k_mg_pre<B, false, MgSet, false><<<g.total_pre, blk, B::SMEM, s>>>(set, c.pre));
+  }
 }
 static void launch_group_pre(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
   if (g.small) launch_group_pre_b<BoxSmall>(g, c, s);
@@ -1550,7 +1625,10 @@ template <class B>
 static void launch_group_post_b(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
   const MgSet set{g.post, g.start_post, g.nbx_post, g.n};
   const char* name = POST_NAMES[g.level < 7 ? g.level : 7];
-  RB_LAUNCH(name, g.bytes_post, s, k_mg_post<B, MgSet><<<g.total_post, dim3(BX, BY), B::SMEM, s>>>(set, c.post));
+  if (g.coded)
+    RB_LAUNCH(name, g.bytes_post, s, k_mg_post<B, MgSet, true><<<g.total_post, dim3(BX, BY), B::SMEM_CODED, s>>>(set, c.post));
+  else
+    RB_LAUNCH(name, g.bytes_post, s, k_mg_post<B, MgSet, false><<<g.total_post, dim3(BX, BY), B::SMEM, s>>>(set, c.post));
 }
 static void launch_group_post(const MgBatchPlan::Group& g, const MgConfig& c, cudaStream_t s) {
   if (g.small) launch_group_post_b<BoxSmall>(g, c, s);

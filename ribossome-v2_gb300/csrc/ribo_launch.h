@@ -175,6 +175,7 @@ struct MgBufs {
   uint8_t* fluid;   // all levels: 1 = water
   float* p_tmp;     // level-0 ping-pong partner of pressure_a (fused path)
   float* p2;        // all levels: pre-smoothed p (fused path)
+  uint8_t* code;    // all levels: neighbour codes from the water flags (null: built per box)
 };
 struct MgConfig {
   int pre, post, coarse, cycles;
@@ -184,6 +185,10 @@ void launch_multigrid(const Dev& d, const MgLevel* levels, int nlevels, const Mg
 // The same V-cycles, bit-identical: fused tile kernels per fine level and one
 // shared-memory kernel for the coarse levels.  Usable when the coarsest level
 // fits in shared memory and 1 <= pre <= 7, 1 <= post <= 8.
+// Neighbour codes of every level (0: not water, else 1 + water neighbours)
+// and the water flags of levels >= 1, from the level-0 flags; run after every
+// wall-mask build.
+void launch_mg_codes(const MgLevel* levels, int nlevels, const MgBufs& b, cudaStream_t s);
 bool multigrid_fused_ok(const MgLevel* levels, int nlevels, const MgConfig& c);
 int multigrid_first_coarse_level(const MgLevel* levels, int nlevels);
 void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nlevels, const MgBufs& b, const MgConfig& c,

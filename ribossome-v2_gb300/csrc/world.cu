@@ -252,7 +252,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   b += 2 * L * 4 * 3;                                             // light, light_next, shade
   b += F * (1 + 8 + 4 + 8 * 3 + 4 * 3 + 4 * 5 + 8 * 3 + 4 + 4);  // mask..heat, mask32, p_tmp
   b += ((size_t)c.fluid_w + c.fluid_h) * 4 + 12 * 4 * 2 + MAX_STEPS * 12 * 4 + 16;
-  b += M * (4 + 4 + 1 + 4);                                       // mg p, rhs, fluid, p2
+  b += M * (4 + 4 + 1 + 4 + 1);                                   // mg p, rhs, fluid, p2, code
   b += 2 * MAX_STEPS * sizeof(ribo_sim_params);
   b += STENCIL_TMAP_BYTES_HOST;                                   // TMA descriptor of the stencil passes
   if (c.precision_mode == RIBO_PRECISION_MIXED) b += mixed_footprint(c, lv);
@@ -327,6 +327,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(mg.fluid, mg_total);
   RB_ALLOC(mg.p_tmp, F * 4);
   RB_ALLOC(mg.p2, mg_total * 4);
+  RB_ALLOC(mg.code, mg_total);
   RB_ALLOC(status, 16);
   {
     void* maps = nullptr;
@@ -353,6 +354,7 @@ ribo_status World::init(const ribo_world_cfg& c) {
   Dev d = dev();
   launch_slope(d, (float)cfg.world_units_per_cell, stream);
   launch_solid_mask(target_one(d, nullptr), stream);
+  launch_mg_codes(levels.data(), (int)levels.size(), mg, stream);
   RB_TRY(cudaGetLastError(), "init kernels");
   RB_TRY(cudaStreamSynchronize(stream), "init");
   return mixed_setup(*this);
@@ -400,6 +402,7 @@ ribo_status World::terrain_changed() {
   Dev d = dev();
   launch_slope(d, (float)cfg.world_units_per_cell, stream);
   launch_solid_mask(target_one(d, nullptr), stream);
+  launch_mg_codes(levels.data(), (int)levels.size(), mg, stream);
   RB_TRY(cudaGetLastError(), "slope/mask");
   ribo_status ms = mixed_setup(*this);
   if (ms != RIBO_OK) return ms;
@@ -502,7 +505,10 @@ void World::record_step(const ribo_sim_params& hp, const ribo_sim_params* P, uin
   }
   uint32_t substep = st.fluid_substep < 1 ? 1 : (st.fluid_substep > 4 ? 4 : st.fluid_substep);
   if (st.fluid_enabled && hp.epoch % substep == 0u) {
-    if (st.terrain_mode) launch_solid_mask(target_one(dev(), P), stream);  // build_solid_mask
+    if (st.terrain_mode) {
+      launch_solid_mask(target_one(dev(), P), stream);  // build_solid_mask
+      launch_mg_codes(levels.data(), (int)levels.size(), mg, stream);
+    }
     launch_temperature(target_one(dev(), P), stream);  // temp_in -> temp_out
     std::swap(temp_cur, temp_nxt);                     // copy_temperature
     std::swap(redox_cur, redox_nxt);
