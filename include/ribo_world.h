@@ -170,7 +170,11 @@ typedef struct ribo_world_cfg {
   uint32_t precision_mode;        // RIBO_PRECISION_*
   uint32_t device;                // CUDA device ordinal the world lives on
   uint32_t no_graphs;             // 1 = never replay step sequences from CUDA graphs
-  uint32_t reserved[4];
+  uint32_t mg_cluster;            // CTAs per cluster of the small multigrid levels' V-cycle launch:
+                                  // 0 automatic (16, else 8, else none), 1 none (a launch per level
+                                  // and the single-CTA coarse kernel), 8 or 16 that size where the
+                                  // device can run it (else none); the same bits every way
+  uint32_t reserved[3];
 } ribo_world_cfg;
 
 enum {

@@ -1410,7 +1410,8 @@ void launch_multigrid_fused(const Dev& d, const MgLevel* levels, int nl, const M
   set_smem_attrs();
   const int cycles = c.cycles < 1 ? 1 : c.cycles;
   {
-    const int nc = cluster_ctas(s);
+    const int avail = cluster_ctas(s);
+    const int nc = c.cluster == 0 ? avail : (c.cluster == 1 || c.cluster > avail ? 0 : c.cluster);
     ClusterPass cp;
     int m = 0;
     size_t smem = 0;

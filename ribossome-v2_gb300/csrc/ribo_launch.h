@@ -179,6 +179,7 @@ struct MgBufs {
 };
 struct MgConfig {
   int pre, post, coarse, cycles;
+  int cluster = 0;  // ribo_world_cfg::mg_cluster
 };
 // One dispatch per half-sweep, restrict and prolong, as the reference records them.
 void launch_multigrid(const Dev& d, const MgLevel* levels, int nlevels, const MgBufs& b, const MgConfig& c, cudaStream_t s);

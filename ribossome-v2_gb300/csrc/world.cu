@@ -459,7 +459,8 @@ void World::pressure_solve(const Dev& d) {
     return;
   }
   if (st.multigrid) {
-    MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, (int)(st.mg_cycles < 1 ? 1 : st.mg_cycles)};
+    MgConfig c{(int)cfg.mg_pre, (int)cfg.mg_post, (int)cfg.mg_coarse, (int)(st.mg_cycles < 1 ? 1 : st.mg_cycles),
+               (int)cfg.mg_cluster};
     if (!st.mg_unfused && multigrid_fused_ok(levels.data(), (int)levels.size(), c))
       launch_multigrid_fused(d, levels.data(), (int)levels.size(), mg, c, stream);
     else
@@ -840,6 +841,8 @@ static ribo_status check_cfg(const ribo_world_cfg* cfg) {
   if ((uint64_t)cfg->grid_w * cfg->grid_h > (1ull << 28))
     return set_error(RIBO_INVALID_ARG, "grid too large (at most 2^28 cells: chem slot indices are u32)");
   if (cfg->precision_mode > RIBO_PRECISION_MIXED) return set_error(RIBO_INVALID_ARG, "unknown precision mode");
+  if (cfg->mg_cluster != 0 && cfg->mg_cluster != 1 && cfg->mg_cluster != 8 && cfg->mg_cluster != 16)
+    return set_error(RIBO_INVALID_ARG, "mg_cluster must be 0 (automatic), 1 (none), 8 or 16");
   return RIBO_OK;
 }
 

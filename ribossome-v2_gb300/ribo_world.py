@@ -59,7 +59,7 @@ class WorldCfg(ctypes.Structure):
         ("world_units_per_cell", ctypes.c_uint32), ("mg_min_size", ctypes.c_uint32),
         ("mg_pre", ctypes.c_uint32), ("mg_post", ctypes.c_uint32), ("mg_coarse", ctypes.c_uint32),
         ("precision_mode", ctypes.c_uint32), ("device", ctypes.c_uint32), ("no_graphs", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 4),
+        ("mg_cluster", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3),
     ]
 
 
@@ -289,14 +289,14 @@ class World:
 
     def __init__(self, grid, fluid=None, seed: int = 1, *, world_units_per_cell: int = 30,
                  mg_min_size: int = 8, mg_pre: int = 2, mg_post: int = 2, mg_coarse: int = 30,
-                 precision_mode: int = 0, device: int = 0, no_graphs: int = 0):
+                 precision_mode: int = 0, device: int = 0, no_graphs: int = 0, mg_cluster: int = 0):
         lib = load_library()
         gw, gh = (grid, grid) if isinstance(grid, int) else grid
         if fluid is None:
             fluid = (gw, gh)
         fw, fh = (fluid, fluid) if isinstance(fluid, int) else fluid
         cfg = WorldCfg(gw, gh, fw, fh, world_units_per_cell, mg_min_size, mg_pre, mg_post, mg_coarse, precision_mode,
-                       device, no_graphs)
+                       device, no_graphs, mg_cluster)
         self.cfg = cfg
         self.gw, self.gh, self.fw, self.fh = gw, gh, fw, fh
         h = ctypes.c_void_p()

@@ -47,7 +47,9 @@ pub struct RiboWorldCfg {
     pub precision_mode: u32,
     pub device: u32,
     pub no_graphs: u32,
-    pub reserved: [u32; 4],
+    /// CTAs per cluster of the small multigrid levels' V-cycle (0 automatic, 1 none, 8, 16).
+    pub mg_cluster: u32,
+    pub reserved: [u32; 3],
 }
 
 #[repr(C)]

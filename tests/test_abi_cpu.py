@@ -103,6 +103,11 @@ def test_invalid_arguments_are_rejected(rw):
     cfg = rw.WorldCfg(1, 1, 1, 1)
     assert lib.ribo_world_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
     assert lib.ribo_world_step(None, None, 1) == 1
+    cfg = rw.WorldCfg(64, 64, 64, 64)
+    cfg.mg_cluster = 4  # 0, 1, 8 or 16
+    n = ctypes.c_uint64()
+    assert lib.ribo_world_footprint(ctypes.byref(cfg), ctypes.byref(n)) == 1
+    assert b"mg_cluster" in lib.ribo_last_error()
 
 
 def _has_gpu():

@@ -218,14 +218,14 @@ def test_async_ledger_readback(rw):
     assert w.poll_ledger() == w.ledger_blocking()
 
 
-def _bench_pair(rw, ro, n, seed=1000):
+def _bench_pair(rw, ro, n, seed=1000, mg_cluster=0):
     """A GPU world and an oracle world with the benchmark's settings: F = G,
     multigrid to 16x16, 4 V-cycles of 3+3 sweeps, 30 coarse sweeps, fluid and
     transport every step, dt = 1, sun heating off, reference defaults (the
     oracle's own table on its side)."""
     import synth
 
-    g = rw.World(n, seed=seed, mg_min_size=16, mg_pre=3, mg_post=3)
+    g = rw.World(n, seed=seed, mg_min_size=16, mg_pre=3, mg_post=3, mg_cluster=mg_cluster)
     o = ro.OracleWorld(n, seed=seed, mg_min_size=16, mg_pre=3, mg_post=3)
     inputs = synth.make_world_inputs(n, seed=seed)
     g.seed_inputs(inputs)
@@ -255,5 +255,21 @@ def test_benchmark_configuration_bit_exact(rw, ro, n, steps):
         o.encode_steps(1)
         compare_worlds(g, o, f"{n}^2 after {s + 1} steps")
     assert g.ledger_blocking() == o.ledger_blocking()
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("cluster", [8, 1], ids=["cluster-8", "no-cluster"])
+@pytest.mark.parametrize("n,steps", [(256, 4), (2048, 1)], ids=["256", "2048"])
+def test_multigrid_cluster_choices_bit_exact(rw, ro, n, steps, cluster):
+    """The small multigrid levels on an 8-CTA cluster (at 256^2 that changes
+    which levels are slabs: 64^2 and 32^2 only) and without a cluster (a box
+    launch per level and the single-CTA coarse kernel), against the oracle:
+    every way of running the V-cycle gives the reference's bits."""
+    g, o = _bench_pair(rw, ro, n, mg_cluster=cluster)
+    for s in range(steps):
+        g.encode_steps(1)
+        o.encode_steps(1)
+        compare_worlds(g, o, f"{n}^2 mg_cluster={cluster} after {s + 1} steps")
     g.close()
     o.close()
