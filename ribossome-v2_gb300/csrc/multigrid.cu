@@ -585,13 +585,10 @@ __device__ __forceinline__ bool coarse_residual(const CLv& L, int y, int x, floa
   return true;
 }
 
-// The V-cycle of a coarse set whose top level (flags, rhs, p) is in shared
-// memory with its codes built: pre-smooth and restrict down to the coarsest
-// level, solve it, prolong and post-smooth back up; the top level's p is
-// left in shared memory.
+// The downward half of a coarse set's V-cycle: pre-smooth and restrict from
+// the top level (in shared memory, codes built) to the coarsest.
 template <bool MP>
-__device__ __forceinline__ void coarse_cycle(const CoarsePass& e, unsigned char* smem, int nu_pre, int nu_post,
-                                             int coarse) {
+__device__ __forceinline__ void coarse_down(const CoarsePass& e, unsigned char* smem, int nu_pre) {
   const CoarseSet& cs = e.cs;
   for (int l = 0; l + 1 < cs.n; l++) {
     const CLv L = coarse_level(cs, smem, l), C = coarse_level(cs, smem, l + 1);
@@ -619,31 +616,13 @@ __device__ __forceinline__ void coarse_cycle(const CoarsePass& e, unsigned char*
     coarse_codes(C);
     __syncthreads();
   }
-  {
-    const CLv L = coarse_level(cs, smem, cs.n - 1);
-    if (MP) {
-      // exact coarsest solve in FP64: one warp per row of the dense inverse
-      // (the inverse indexes the level's cells in row-major order)
-      const int nc = L.nx * L.ny;
-      float* rn = reinterpret_cast<float*>(smem + (size_t)10 * cs.total);
-      for (int i = threadIdx.x; i < nc; i += COARSE_THREADS) rn[i] = L.R[L.at(i / L.nx, i % L.nx)];
-      __syncthreads();
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int i = warp; i < nc; i += COARSE_THREADS / 32) {
-        const double* row = e.inv + (size_t)i * nc;
-        double acc = 0.0;
-        for (int j = lane; j < nc; j += 32) acc += row[j] * (double)rn[j];
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane == 0) L.P[L.at(i / L.nx, i % L.nx)] = (float)acc;
-      }
-      __syncthreads();
-    } else {
-      for (int k = 0; k < coarse; k++) {
-        coarse_sweep(L, 0);
-        coarse_sweep(L, 1);
-      }
-    }
-  }
+}
+
+// The upward half: prolong the coarser level's correction and post-smooth,
+// up to the top level, whose p is left in shared memory.
+template <bool MP>
+__device__ __forceinline__ void coarse_up(const CoarsePass& e, unsigned char* smem, int nu_post) {
+  const CoarseSet& cs = e.cs;
   for (int l = cs.n - 2; l >= 0; l--) {
     const CLv L = coarse_level(cs, smem, l), C = coarse_level(cs, smem, l + 1);
     for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
@@ -662,13 +641,58 @@ __device__ __forceinline__ void coarse_cycle(const CoarsePass& e, unsigned char*
   }
 }
 
-template <class S, bool MP = false>
-__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ S s, int nu_pre, int nu_post, int coarse) {
-  const CoarsePass& e = coarse_of(s);
+// Rows [i0, i1) of the exact FP64 coarsest solve: p_i = sum_j inv[i][j] rhs_j
+// (the inverse indexes the level's cells in row-major order), one warp per
+// row, stored at the cell's place in `P` (L's p plane, in this CTA or, through
+// distributed shared memory, in another one).
+__device__ __forceinline__ void coarsest_dense_rows(const CoarsePass& e, const CLv& L, const float* rn, float* P, int i0,
+                                                    int i1) {
+  const int nc = L.nx * L.ny;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = i0 + warp; i < i1; i += COARSE_THREADS / 32) {
+    const double* row = e.inv + (size_t)i * nc;
+    double acc = 0.0;
+    for (int j = lane; j < nc; j += 32) acc += row[j] * (double)rn[j];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) P[L.at(i / L.nx, i % L.nx)] = (float)acc;
+  }
+}
+
+// The V-cycle of a coarse set whose top level (flags, rhs, p) is in shared
+// memory with its codes built: down to the coarsest level, its solve (the
+// reference's sweeps, or in the mixed-precision form the exact FP64 solve
+// with the dense inverse), and back up; the top level's p is left in shared
+// memory.
+template <bool MP>
+__device__ __forceinline__ void coarse_cycle(const CoarsePass& e, unsigned char* smem, int nu_pre, int nu_post,
+                                             int coarse) {
+  const CoarseSet& cs = e.cs;
+  coarse_down<MP>(e, smem, nu_pre);
+  {
+    const CLv L = coarse_level(cs, smem, cs.n - 1);
+    if (MP) {
+      const int nc = L.nx * L.ny;
+      float* rn = reinterpret_cast<float*>(smem + (size_t)10 * cs.total);
+      for (int i = threadIdx.x; i < nc; i += COARSE_THREADS) rn[i] = L.R[L.at(i / L.nx, i % L.nx)];
+      __syncthreads();
+      coarsest_dense_rows(e, L, rn, L.P, 0, nc);
+      __syncthreads();
+    } else {
+      for (int k = 0; k < coarse; k++) {
+        coarse_sweep(L, 0);
+        coarse_sweep(L, 1);
+      }
+    }
+  }
+  coarse_up<MP>(e, smem, nu_post);
+}
+
+// Clears a coarse set's planes (rings and rows outside stay non-water, p =
+// rhs = 0), loads its top level (the world's own pressure_a, divergence and
+// wall mask when the top is level 0) and builds the top level's codes.
+__device__ __forceinline__ void coarse_load_top(const CoarsePass& e, unsigned char* smem) {
   const CoarseSet& cs = e.cs;
   const bool TOP = e.top != 0;
-  extern __shared__ __align__(16) unsigned char smem[];
-  // every plane cell starts as non-water, p = rhs = 0 (the rings stay so)
   {
     float* f = reinterpret_cast<float*>(smem);
     for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) f[i] = 0.0f;
@@ -676,40 +700,49 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_const
     for (int i = threadIdx.x; i < 2 * cs.total; i += COARSE_THREADS) b[i] = 0;
   }
   __syncthreads();
-  {
-    const CLv L = coarse_level(cs, smem, 0);
-    for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
-      const int y = idx / L.nx, x = idx - y * L.nx;
-      uint8_t f;
-      float r, p = 0.0f;
-      if (TOP) {
-        const size_t gi = (size_t)y * e.fw + x;
-        f = e.mask[gi] ? 0 : 1;
-        r = e.div[gi];
-        p = f ? e.pa[gi] : 0.0f;
-      } else {
-        f = cs.fl_top[idx];
-        r = cs.rhs_top[idx];
-      }
-      const int a = L.at(y, x);
-      L.F[a] = f;
-      L.P[a] = f ? p : 0.0f;
-      L.R[a] = f ? r : 0.0f;
+  const CLv L = coarse_level(cs, smem, 0);
+  for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
+    const int y = idx / L.nx, x = idx - y * L.nx;
+    uint8_t f;
+    float r, p = 0.0f;
+    if (TOP) {
+      const size_t gi = (size_t)y * e.fw + x;
+      f = e.mask[gi] ? 0 : 1;
+      r = e.div[gi];
+      p = f ? e.pa[gi] : 0.0f;
+    } else {
+      f = cs.fl_top[idx];
+      r = cs.rhs_top[idx];
     }
-    __syncthreads();
-    coarse_codes(L);
-    __syncthreads();
+    const int a = L.at(y, x);
+    L.F[a] = f;
+    L.P[a] = f ? p : 0.0f;
+    L.R[a] = f ? r : 0.0f;
   }
+  __syncthreads();
+  coarse_codes(L);
+  __syncthreads();
+}
+
+// Stores the top level's p (to pressure_a when the top is level 0).
+__device__ __forceinline__ void coarse_store_top(const CoarsePass& e, unsigned char* smem) {
+  const CoarseSet& cs = e.cs;
+  const CLv L = coarse_level(cs, smem, 0);
+  for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
+    const int y = idx / L.nx, x = idx - y * L.nx;
+    const float v = L.P[L.at(y, x)];
+    if (e.top) e.pa[(size_t)y * e.fw + x] = v;
+    else cs.p_out[idx] = v;
+  }
+}
+
+template <class S, bool MP = false>
+__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(const __grid_constant__ S s, int nu_pre, int nu_post, int coarse) {
+  const CoarsePass& e = coarse_of(s);
+  extern __shared__ __align__(16) unsigned char smem[];
+  coarse_load_top(e, smem);
   coarse_cycle<MP>(e, smem, nu_pre, nu_post, coarse);
-  {
-    const CLv L = coarse_level(cs, smem, 0);
-    for (int idx = threadIdx.x; idx < L.nx * L.ny; idx += COARSE_THREADS) {
-      const int y = idx / L.nx, x = idx - y * L.nx;
-      const float v = L.P[L.at(y, x)];
-      if (TOP) e.pa[(size_t)y * e.fw + x] = v;
-      else cs.p_out[idx] = v;
-    }
-  }
+  coarse_store_top(e, smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -774,6 +807,11 @@ __device__ __forceinline__ void cluster_sync() {
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_ctas() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;\n" : "=r"(r));
   return r;
 }
 // The address of `p` (this CTA's shared memory) in CTA `rank` of the cluster.
@@ -1085,6 +1123,44 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1)
       if (TOP) e.pa[(size_t)y * e.fw + x] = v;
       else cp.p_out[(size_t)y * L.nx + x] = v;
     }
+  }
+}
+
+// The mixed-precision preconditioner's coarse V-cycle with its exact FP64
+// coarsest solve spread over a thread-block cluster: CTA 0 runs the levels
+// (down, then up, as k_mg_coarse does); for the solve every CTA takes a share
+// of the rows of the dense inverse, multiplies them with the coarsest
+// right-hand side (copied from CTA 0 through distributed shared memory) in
+// the same order as one CTA would, and stores its part of the solution into
+// CTA 0's plane.  The FP64 products and the inverse's loads then run on NC
+// SMs instead of one.
+__global__ void __launch_bounds__(COARSE_THREADS, 1)
+    k_mp_coarse_cluster(const __grid_constant__ CoarseOne s, int nu_pre, int nu_post) {
+  const CoarsePass& e = s.e;
+  const CoarseSet& cs = e.cs;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t rank = cluster_rank(), ncta = cluster_ctas();
+  const CLv L = coarse_level(cs, smem, cs.n - 1);
+  const int nc = L.nx * L.ny;
+  float* rn = reinterpret_cast<float*>(smem + (size_t)10 * cs.total);
+  if (rank == 0) {
+    coarse_load_top(e, smem);
+    coarse_down<true>(e, smem, nu_pre);
+    for (int i = threadIdx.x; i < nc; i += COARSE_THREADS) rn[i] = L.R[L.at(i / L.nx, i % L.nx)];
+  }
+  cluster_sync();  // the coarsest right-hand side is ready (and every CTA has started)
+  if (rank != 0) {
+    const float* r0 = cta_map(rn, 0u);
+    for (int i = threadIdx.x; i < nc; i += COARSE_THREADS) rn[i] = r0[i];
+    __syncthreads();
+  }
+  const int per = (nc + (int)ncta - 1) / (int)ncta;
+  const int i0 = min(nc, (int)rank * per), i1 = min(nc, i0 + per);
+  coarsest_dense_rows(e, L, rn, cta_map(L.P, 0u), i0, i1);
+  cluster_sync();  // the solution is complete in CTA 0; no CTA reads another after this
+  if (rank == 0) {
+    coarse_up<true>(e, smem, nu_post);
+    coarse_store_top(e, smem);
   }
 }
 
@@ -1859,7 +1935,39 @@ void mp_launch_post(const MpLevelArgs& a, const MgLevel& L, int l, bool top, boo
 
 }  // namespace
 
-void multigrid_prepare_mixed() { set_smem_attrs(); }
+// CTAs per cluster for k_mp_coarse_cluster on this device (16, else 8; 0: one
+// CTA), queried when a mixed-precision world is created (outside capture).
+static std::atomic<int> g_mp_cluster[64];
+void multigrid_prepare_mixed() {
+  set_smem_attrs();
+  const int dev = DeviceOnce::device();
+  if (g_mp_cluster[dev].load(std::memory_order_acquire) != 0) return;
+  int found = -1;
+  if (cudaFuncSetAttribute(k_mp_coarse_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COARSE_SMEM_MAX) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(k_mp_coarse_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    for (int nc : {16, 8}) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)nc;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)nc);
+      cfg.blockDim = dim3(COARSE_THREADS);
+      cfg.dynamicSmemBytes = COARSE_SMEM_MAX;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, k_mp_coarse_cluster, &cfg) == cudaSuccess && n >= 1) {
+        found = nc;
+        break;
+      }
+    }
+  }
+  cudaGetLastError();
+  g_mp_cluster[dev].store(found, std::memory_order_release);
+}
 
 size_t mixed_vcycle_tiles(const MgLevel* levels, int nl, const MgConfig& c) {
   (void)nl;
@@ -1906,8 +2014,25 @@ int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBuf
   CoarseOne co{coarse_pass(d, levels, nl, b, &coarse_smem, &coarse_bytes)};
   co.e.inv = h.coarse_inv;
   co.e.alpha = h.alpha;
-  RB_LAUNCH("mp_coarse_vcycle", coarse_bytes, s,
-            k_mg_coarse<CoarseOne, true><<<1, COARSE_THREADS, coarse_smem, s>>>(co, h.pre, h.post, 0));
+  const int ncl = g_mp_cluster[DeviceOnce::device()].load(std::memory_order_acquire);
+  if (ncl > 0) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)ncl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)ncl);
+    cfg.blockDim = dim3(COARSE_THREADS);
+    cfg.dynamicSmemBytes = coarse_smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RB_LAUNCH("mp_coarse_vcycle", coarse_bytes, s, cudaLaunchKernelEx(&cfg, k_mp_coarse_cluster, co, h.pre, h.post));
+  } else {
+    RB_LAUNCH("mp_coarse_vcycle", coarse_bytes, s,
+              k_mg_coarse<CoarseOne, true><<<1, COARSE_THREADS, coarse_smem, s>>>(co, h.pre, h.post, 0));
+  }
   for (int l = k - 1; l >= 0; l--) {
     const MpLevelArgs a = args(l);
     const bool half = l < h.nhalf;
