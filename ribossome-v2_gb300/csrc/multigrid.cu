@@ -1756,7 +1756,7 @@ namespace {
 struct MpLevelArgs {
   int nx, ny;
   float eps;
-  const uint8_t* fl;  // water flags of the level
+  const uint8_t* code;  // neighbour codes of the level (0: not water)
   const void* rhs;    // right-hand side (type T); level 0: the CG residual (float)
   void* ef;           // pre-smoothed correction (type T)
   int cnx, cny;
@@ -1799,8 +1799,8 @@ __global__ void __launch_bounds__(BX* BY) k_mp_pre(const __grid_constant__ MpLev
   const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
   const RbSmem<B> Sm(smem_raw, (x0 + y0) & 1);
   const float sc = TOP ? a.scale[0] : 1.0f;
-  rb_load<B>(Sm, x0 - H, y0 - H, a.nx, a.ny, [&](bool in, size_t gi, int, int, uint8_t& f, float& r, float& p) {
-    f = in ? a.fl[gi] : 0;
+  rb_load<B, true>(Sm, x0 - H, y0 - H, a.nx, a.ny, [&](bool in, size_t gi, int, int, uint8_t& f, float& r, float& p) {
+    f = in ? a.code[gi] : 0;
     r = mp_rhs<TOP, T>(a, gi, sc);
     p = 0.0f;
   });
@@ -1835,8 +1835,8 @@ __global__ void __launch_bounds__(BX* BY) k_mp_post(const __grid_constant__ MpLe
   const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
   const RbSmem<B> Sm(smem_raw, (x0 + y0) & 1);
   const float sc = TOP ? a.scale[0] : 1.0f;
-  rb_load<B>(Sm, x0 - H, y0 - H, a.nx, a.ny, [&](bool in, size_t gi, int gx, int gy, uint8_t& f, float& r, float& p) {
-    f = in ? a.fl[gi] : 0;
+  rb_load<B, true>(Sm, x0 - H, y0 - H, a.nx, a.ny, [&](bool in, size_t gi, int gx, int gy, uint8_t& f, float& r, float& p) {
+    f = in ? a.code[gi] : 0;
     r = mp_rhs<TOP, T>(a, gi, sc);
     const size_t ci = in ? (size_t)(gy / 2) * a.cnx + gx / 2 : 0;
     p = mp_ld(static_cast<const T*>(a.ef), gi) + a.alpha * a.cE[ci];
@@ -1907,7 +1907,7 @@ template <class B>
 void mp_launch_pre(const MpLevelArgs& a, const MgLevel& L, int l, bool top, bool half, bool chalf, int nu, cudaStream_t s) {
   const TileGrid t = tile_grid<B>(L, 2 * nu + 1);
   const dim3 grid(t.nbx, t.nby), blk(BX, BY);
-  const size_t sm = B::SMEM;
+  const size_t sm = B::SMEM_CODED;
   const double es = half ? 2.0 : 4.0, n = (double)a.nx * a.ny;
   const double bytes = n * ((top ? 9.0 : es + 1.0) + es + (chalf ? 2.0 : 4.0) / 4.0);
   const char* name = MP_PRE_NAMES[l < 7 ? l : 7];
@@ -1923,7 +1923,7 @@ template <class B>
 void mp_launch_post(const MpLevelArgs& a, const MgLevel& L, int l, bool top, bool half, int nu, cudaStream_t s) {
   const TileGrid t = tile_grid<B>(L, 2 * nu);
   const dim3 grid(t.nbx, t.nby), blk(BX, BY);
-  const size_t sm = B::SMEM;
+  const size_t sm = B::SMEM_CODED;
   const double es = half ? 2.0 : 4.0, n = (double)a.nx * a.ny;
   const double bytes = n * (es + (top ? 9.0 : es + 1.0) + 1.0 + (top ? 8.0 : 4.0));
   const char* name = MP_POST_NAMES[l < 7 ? l : 7];
@@ -1985,7 +1985,7 @@ int launch_mixed_vcycle(const Dev& d, const MgLevel* levels, int nl, const MgBuf
     a.nx = levels[l].nx;
     a.ny = levels[l].ny;
     a.eps = levels[l].eps;
-    a.fl = b.fluid + levels[l].off;
+    a.code = b.code + levels[l].off;
     a.rhs = l == 0 ? static_cast<const void*>(h.r) : h.fine[l].rhs;
     a.ef = h.fine[l].ef;
     a.cnx = levels[l + 1].nx;
