@@ -86,8 +86,7 @@ struct Dev {
   float* light_next;  // light_propagate's output (the light block; the light field itself is written through light)
   const uint32_t* shade;
   float2* slope;
-  uint32_t* agg_act;
-  uint32_t* agg_nb;
+  uint32_t* agg_nb;   // 3 x 3 box sums of the activated counts (aggregation)
   // fluid-resolution buffers
   uint8_t* mask;    // 1 = wall
   float2* normal;   // outward wall normal of each fluid cell (from the mask)
@@ -112,7 +111,7 @@ struct Dev {
   uint32_t* status;   // error bits written by kernels instead of trapping (RIBO_ERR_*)
   const void* tmap;   // TMA descriptors of the stencil passes' tiles (csrc/ribo_tma.cuh), or null
 };
-static_assert(sizeof(Dev) == 16 * 4 + 31 * sizeof(void*), "Dev has no padding bytes: every byte is a member");
+static_assert(sizeof(Dev) == 16 * 4 + 30 * sizeof(void*), "Dev has no padding bytes: every byte is a member");
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }

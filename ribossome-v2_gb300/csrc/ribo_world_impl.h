@@ -78,7 +78,7 @@ struct World {
   bool light_dirty = true;      // the next light block is a full sweep (creation, gamma upload, light turned on)
   uint32_t* shade = nullptr;
   float2* slope = nullptr;
-  uint32_t *agg_act = nullptr, *agg_nb = nullptr;
+  uint32_t* agg_nb = nullptr;
   // terrain grains (terrain_mode 1 and the brush)
   uint8_t* terrain_code = nullptr;
   uint8_t* terrain_arrivals = nullptr;

@@ -65,44 +65,40 @@ __global__ void k_thermal(const __grid_constant__ S s) {
   }
 }
 
-// transport.wgsl:61-68
+// agg_count + agg_neighbours (transport.wgsl:61-87) in one pass.  The
+// scatter reads a cell's neighbour count plus its own activated count
+// (transport.wgsl:196-201); integer adds commute, so each cell stores that sum
+// directly: the 3 x 3 box of activated counts.  A CTA counts the activated
+// monomers of its 32 x 8 tile and one-cell ring into shared memory (cells off
+// the grid count 0, as the reference skips them) and sums the boxes there.
 template <class S>
-__global__ void k_agg_count(const __grid_constant__ S s) {
+__global__ void k_agg(const __grid_constant__ S s) {
   RB_WORLD(s);
-  // four cells per thread, LINEAR_THREADS apart, loaded together
-  const size_t n = (size_t)d.gw * d.gh, i0 = (size_t)cta.bx * 4 * blockDim.x + threadIdx.x;
-  uint4 c[4];
+  constexpr int W = BX + 2, N = W * (BY + 2), NT = BX * BY;
+  static_assert(N <= 2 * NT, "two cells of the tile and ring per thread");
+  __shared__ uint32_t act[N];
+  const int x0 = (int)cta.bx * BX - 1, y0 = (int)cta.by * BY - 1, tid = threadIdx.y * BX + threadIdx.x;
+  uint4 c[2];
+  bool in[2];
 #pragma unroll
-  for (int r = 0; r < 4; r++) {
-    const size_t i = i0 + (size_t)r * blockDim.x;
-    c[r] = load_cell(d.chem, i < n ? i : n - 1);
+  for (int u = 0; u < 2; u++) {  // both loads before either store
+    const int i = tid + u * NT, gx = x0 + i % W, gy = y0 + i / W;
+    in[u] = i < N && gx >= 0 && gy >= 0 && gx < d.gw && gy < d.gh;
+    c[u] = in[u] ? load_cell(d.chem, (size_t)gy * d.gw + gx) : make_uint4(0u, 0u, 0u, 0u);
   }
 #pragma unroll
-  for (int r = 0; r < 4; r++) {
-    const size_t i = i0 + (size_t)r * blockDim.x;
-    if (i < n)
-      d.agg_act[i] = (c[r].x & CHEM_STATE_MASK) + (c[r].y & CHEM_STATE_MASK) + (c[r].z & CHEM_STATE_MASK) +
-                     (c[r].w & CHEM_STATE_MASK);
+  for (int u = 0; u < 2; u++) {
+    const int i = tid + u * NT;
+    if (i < N)
+      act[i] = (c[u].x & CHEM_STATE_MASK) + (c[u].y & CHEM_STATE_MASK) + (c[u].z & CHEM_STATE_MASK) +
+               (c[u].w & CHEM_STATE_MASK);
   }
-}
-// transport.wgsl:71-87.  The scatter reads the neighbour count plus the
-// cell's own activated count (transport.wgsl:196-201); integer adds
-// commute, so agg_nb holds that sum directly: the 3 x 3 box of activated
-// counts.
-template <class S>
-__global__ void k_agg_neighbours(const __grid_constant__ S s) {
-  RB_WORLD(s);
-  int x = cta.bx * BX + threadIdx.x, y = cta.by * BY + threadIdx.y;
+  __syncthreads();
+  const int x = x0 + 1 + (int)threadIdx.x, y = y0 + 1 + (int)threadIdx.y;
   if (x >= d.gw || y >= d.gh) return;
-  uint32_t sum = d.agg_act[(size_t)y * d.gw + x];
-  for (int dy = -1; dy <= 1; dy++)
-    for (int dx = -1; dx <= 1; dx++) {
-      if (dx == 0 && dy == 0) continue;
-      int nx = x + dx, ny = y + dy;
-      if (nx < 0 || ny < 0 || nx >= d.gw || ny >= d.gh) continue;
-      sum += d.agg_act[(size_t)ny * d.gw + nx];
-    }
-  d.agg_nb[(size_t)y * d.gw + x] = sum;
+  const int b = ((int)threadIdx.y + 1) * W + (int)threadIdx.x + 1;
+  d.agg_nb[(size_t)y * d.gw + x] = act[b - W - 1] + act[b - W] + act[b - W + 1] + act[b - 1] + act[b] + act[b + 1] +
+                                   act[b + W - 1] + act[b + W] + act[b + W + 1];
 }
 
 // transport.wgsl:260-273 (fluid_velocity_at_world, reading velocity_a)
@@ -970,8 +966,7 @@ void launch_thermal(const Target& t, cudaStream_t s) {
   RB_PASS("thermal_activation", 4.0 * t.fcells, s, t, GEO_ENV_TALL, dim3(BX, BY), 0, k_thermal, nullptr);
 }
 void launch_agg(const Target& t, cudaStream_t s) {
-  RB_PASS("agg_count", 20.0 * t.cells, s, t, GEO_ENV_LINEAR4, dim3(LINEAR_THREADS), 0, k_agg_count, nullptr);
-  RB_PASS("agg_neighbours", 8.0 * t.cells, s, t, GEO_ENV, dim3(BX, BY), 0, k_agg_neighbours, nullptr);
+  RB_PASS("aggregation_counts", 20.0 * t.cells, s, t, GEO_ENV, dim3(BX, BY), 0, k_agg, nullptr);
 }
 void launch_scatter(const Target& t, bool simple, cudaStream_t s) {
   const double bytes = 45.0 * t.cells + 12.0 * t.fcells;

@@ -168,7 +168,6 @@ Dev World::dev() const {
   d.light_next = light_next;
   d.shade = shade;
   d.slope = slope;
-  d.agg_act = agg_act;
   d.agg_nb = agg_nb;
   d.mask = mask;
   d.normal = normal;
@@ -247,7 +246,7 @@ size_t world_footprint(const ribo_world_cfg& c) {
   std::vector<MgLevel> lv;
   const size_t M = build_levels((int)c.fluid_w, (int)c.fluid_h, c.mg_min_size ? c.mg_min_size : 8, lv);
   size_t b = 0;
-  b += C * (16 + 16 + 4 + 8 + 4 + 4);                             // chem a/b, gamma, slope, agg_act, agg_nb
+  b += C * (16 + 16 + 4 + 8 + 4);                                 // chem a/b, gamma, slope, agg_nb
   b += 2 * C + terrain_list_entries((int)c.grid_w, (int)c.grid_h) * 4 + 64;  // terrain codes, arrivals, lists, counts
   b += 2 * L * 4 * 3;                                             // light, light_next, shade
   b += F * (1 + 8 + 4 + 8 * 3 + 4 * 3 + 4 * 5 + 8 * 3 + 4 + 4);  // mask..heat, mask32, p_tmp
@@ -286,7 +285,6 @@ ribo_status World::init(const ribo_world_cfg& c) {
   RB_ALLOC(shade, 2 * L * 4);
   RB_ALLOC(light_next, 2 * L * 4);
   RB_ALLOC(slope, C * 8);
-  RB_ALLOC(agg_act, C * 4);
   RB_ALLOC(agg_nb, C * 4);
   RB_ALLOC(terrain_code, C);
   RB_ALLOC(terrain_arrivals, C);

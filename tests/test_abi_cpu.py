@@ -159,7 +159,7 @@ def test_world_footprint_counts_every_buffer(rw):
                 break
         terrain = 2 * C + 36 * ((gw + 2) // 3) * ((gh + 2) // 3) + 64
         tmaps = 128  # TMA descriptor of the stencil passes
-        want = C * 52 + terrain + 24 * L + F * 101 + (fw + fh) * 4 + 96 + 64 * 48 + 16 + M * 14 + 2 * 64 * 464 + tmaps
+        want = C * 48 + terrain + 24 * L + F * 101 + (fw + fh) * 4 + 96 + 64 * 48 + 16 + M * 14 + 2 * 64 * 464 + tmaps
         assert rw.world_footprint((gw, gh), (fw, fh), mg_min_size=mg) == want
 
 
