@@ -809,7 +809,7 @@ __device__ __forceinline__ uint32_t cluster_rank() {
   asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
   return r;
 }
-__device__ __forceinline__ uint32_t cluster_ctas() {
+__device__ __forceinline__ uint32_t cluster_size() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_nctarank;\n" : "=r"(r));
   return r;
@@ -1139,7 +1139,7 @@ __global__ void __launch_bounds__(COARSE_THREADS, 1)
   const CoarsePass& e = s.e;
   const CoarseSet& cs = e.cs;
   extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t rank = cluster_rank(), ncta = cluster_ctas();
+  const uint32_t rank = cluster_rank(), ncta = cluster_size();
   const CLv L = coarse_level(cs, smem, cs.n - 1);
   const int nc = L.nx * L.ny;
   float* rn = reinterpret_cast<float*>(smem + (size_t)10 * cs.total);
